@@ -1,0 +1,425 @@
+#!/usr/bin/env python
+"""Benchmark of the simulation step on the 256^3 APIC workload.
+
+Workload (fill256_apic): 256^3 MAC grid in the unit cube, solid walls on all
+six faces; fluid fills every interior cell with centre y < 0.5 (8 jittered
+particles per cell, seed 0, 65.5M particles, FP32 SoA, APIC C as 9 FP32);
+a solid sphere of radius 0.15 at (0.5 + 0.1 sin(pi t), 0.6, 0.5); a disc source
+of radius 4 cells at y = 0.95 emitting 8 jittered particles per covered cell
+per step with velocity (0, -1, 0); an 8x8x8-cell sink box at the floor corner
+(0, 0, 0); dt = 1/480 s; PCG to relative residual 1e-6 (max 2000 iterations)
+from zero pressure, as the reference starts.  All inputs are synthetic and
+seeded; no dataset is involved.
+
+A "step" is one Simulator::simulate(dt).  `value` is steps/s with the state
+resident in HBM (8.6 GB of particle state, far larger than the 129 MB L2, so
+no L2 flush is needed between steps); `e2e` is the same metric through the C
+ABI with the renderer hand-off of every step (fsim_fill_gfx into pinned host
+memory, SimulationManager::getParticleGfxData) inside the timed region.
+
+--impl reference times the reference's algorithm on the host cores: the FP64
+oracle (oracle/fsim_oracle.c, a bit-exact restatement of the reference's
+Simulator pinned by tests/golden) with all OpenMP threads, on the same
+workload.  Each of its steps takes tens of seconds, so it times min(K, 2)
+steps after one warm-up step and says so in its line.
+
+Multi-GPU: the step does not shard (every PCG iteration needs halo exchange and
+global reductions), so --gpus N runs N independent replicas, one per GPU, and
+`value` sums their steps/s ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "fill256_apic"
+
+
+# ---------------------------------------------------------------- workload
+def workload_scene(res: int = 256):
+    from fluid_simulator_gb300.scenes import GridSpec, fill_below
+
+    grid = GridSpec(res)
+    return grid, fill_below(grid, 0.5, seed=0)
+
+
+def obstacles_at(t: float, dt: float, h: float, N):
+    """Sphere moving in x, disc source, corner sink box (fsim obstacle structs)."""
+    x = 0.5 + 0.1 * math.sin(math.pi * t)
+    xp = 0.5 + 0.1 * math.sin(math.pi * (t - dt))
+    return [
+        N.obstacle(N.OBS_SPHERE, (x, 0.6, 0.5), r=0.15, prev_pos=(xp, 0.6, 0.5), speed=((x - xp) / dt, 0.0, 0.0)),
+        N.obstacle(N.OBS_DISC_SOURCE, (0.5, 0.95, 0.5), r=4 * h, spawn_speed=-1.0),
+        N.obstacle(N.OBS_BOX_SINK, (4 * h, 4 * h, 4 * h), size=(8 * h, 8 * h, 8 * h)),
+    ]
+
+
+# ---------------------------------------------------------------- helpers
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, path: str, gpu: int):
+        self.path = path
+        self.proc = None
+        self.gpu = gpu
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cudart():
+    for name in ("libcudart.so.13", "libcudart.so"):
+        try:
+            return C.CDLL(name)
+        except OSError:
+            pass
+    import glob
+
+    return C.CDLL(sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*"))[0])
+
+
+class Events:
+    """CUDA events on the library's stream (cudart through ctypes)."""
+
+    def __init__(self, rt, stream):
+        self.rt, self.stream = rt, stream
+        self.a, self.b = C.c_void_p(), C.c_void_p()
+        rt.cudaEventCreate(C.byref(self.a))
+        rt.cudaEventCreate(C.byref(self.b))
+
+    def start(self):
+        self.rt.cudaEventRecord(self.a, C.c_void_p(self.stream))
+
+    def stop_ms(self):
+        self.rt.cudaEventRecord(self.b, C.c_void_p(self.stream))
+        self.rt.cudaEventSynchronize(self.b)
+        ms = C.c_float()
+        self.rt.cudaEventElapsedTime(C.byref(ms), self.a, self.b)
+        return ms.value
+
+
+# algorithmic bytes (FP32 SoA, each array counted once per stage; sort traffic excluded)
+BYTES_PER_PARTICLE = {0: 84, 1: 96, 2: 156}   # PIC, FLIP, APIC per step
+BYTES_P2G_PER_PARTICLE = {0: 24, 1: 24, 2: 60}  # read pos, v (+C)
+BYTES_P2G_PER_CELL = 17                        # write 3 face v + flag + avgPNum
+BYTES_G2P_PER_PARTICLE = {0: 24, 1: 36, 2: 60}
+BYTES_G2P_PER_CELL = {0: 12, 1: 24, 2: 12}
+BYTES_GRID_PER_CELL = 150
+BYTES_PCG_PER_FLUID_CELL_ITER = 60
+
+
+def dist_setup(n_gpus: int):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # only for the barrier / max over replicas
+
+        dist.init_process_group("gloo")
+    return rank, world, local, dist
+
+
+def dist_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- our arm
+def run_fsim(args):
+    from fluid_simulator_gb300 import native as N
+
+    rank, world, local, dist = dist_setup(args.gpus)
+    rt = cudart()
+    rt.cudaSetDevice(local)
+    res = args.res
+    grid, pos = workload_scene(res)
+    h = grid.h
+    dt = 1.0 / 480.0 if res == 256 else 1.0 / (480.0 * res / 256.0)
+    p = N.default_params(transfer=N.APIC, resolution=res, tol=1e-6, tol_mode=N.TOL_REL_L2, max_iters=2000,
+                         spawning=True, despawning=True, timing=True, precision=N.PREC_MIXED,
+                         warm_start=N.WARM_ZERO)
+    sim = N.Simulation(res, p)
+    sim.set_particles(pos)
+    del pos
+    t = 0.0
+
+    def step():
+        nonlocal t
+        sim.set_obstacles(obstacles_at(t, dt, h, N))
+        st = sim.step(dt)
+        t += dt
+        return st
+
+    for _ in range(args.warmup):
+        step()
+    stream = sim.lib.fsim_stream(sim.ctx)
+    ev = Events(rt, stream)
+    stats = []
+    barrier(dist)
+    sim.synchronize()
+    with ClockSampler(os.path.join(args.out_dir, f"clocks_rank{rank}.csv"), local) as clk:
+        ev.start()
+        for _ in range(args.steps):
+            stats.append(step())
+        ms = ev.stop_ms()
+    sim.synchronize()
+    barrier(dist)
+    ms_max = dist_max(dist, ms)
+    clocks = clk.summary()
+
+    # end to end through the C ABI with the renderer hand-off in pinned host memory
+    n_cap = int(sim.n * 1.2) + 1_000_000
+    gfx = (N.ParticleGfx * n_cap)()
+    rt.cudaHostRegister(C.cast(gfx, C.c_void_p), C.c_size_t(C.sizeof(gfx)), 0)
+    e2e_steps = max(1, min(args.steps, 5))
+    d2h = 0
+    h2d = 0
+    barrier(dist)
+    ev.start()
+    for _ in range(e2e_steps):
+        obs = obstacles_at(t, dt, h, N)
+        h2d += len(obs) * C.sizeof(N.Obstacle)
+        sim.set_obstacles(obs)
+        sim.step(dt)
+        t += dt
+        got = C.c_int64()
+        rc = sim.lib.fsim_fill_gfx(sim.ctx, gfx, n_cap, C.byref(got), N.HOST)
+        if rc != 0:
+            raise RuntimeError("fsim_fill_gfx failed")
+        d2h += got.value * C.sizeof(N.ParticleGfx)
+    e2e_ms = ev.stop_ms()
+    barrier(dist)
+    e2e_ms = dist_max(dist, e2e_ms)
+    rt.cudaHostUnregister(C.cast(gfx, C.c_void_p))
+
+    # per-stage breakdown (library events)
+    def mean(key):
+        return statistics.mean(getattr(s, key) for s in stats)
+
+    np_mean = mean("num_particles")
+    its = mean("pcg_iterations")
+    ms_step = ms_max / args.steps
+    value = world * args.steps / (ms_max / 1000.0)
+    peak, peak_kind = load_peaks()
+    ncell = res ** 3
+    nfluid_est = mean("num_active_bricks") * 256
+    # roofline of the dominant kernel class: the PCG iteration (three kernels) at 60 B/fluid cell
+    pcg_ms_per_it = (mean("ms_solve") - mean("ms_pcg_setup")) / max(1.0, its)
+    g2p_bytes = np_mean * BYTES_G2P_PER_PARTICLE[2] + ncell * BYTES_G2P_PER_CELL[2]
+    p2g_bytes = np_mean * BYTES_P2G_PER_PARTICLE[2] + ncell * BYTES_P2G_PER_CELL
+    kernels = {
+        "g2p": {"ms": mean("ms_g2p_kernel"), "bytes": g2p_bytes},
+        "p2g": {"ms": mean("ms_p2g_kernel"), "bytes": p2g_bytes},
+    }
+    for k in kernels.values():
+        k["gbs"] = k["bytes"] / (k["ms"] / 1e3) / 1e9 if k["ms"] > 0 else None
+        k["frac"] = k["gbs"] / peak if k["gbs"] else None
+    dominant = "g2p" if kernels["g2p"]["ms"] >= kernels["p2g"]["ms"] else "p2g"
+    dk = kernels[dominant]
+    step_bytes = np_mean * BYTES_PER_PARTICLE[2] + ncell * BYTES_GRID_PER_CELL + \
+        its * nfluid_est * BYTES_PCG_PER_FLUID_CELL_ITER
+    line = {
+        "metric": "steps/s (256^3 APIC step, PCG to 1e-6 relative residual)",
+        "value": round(value, 4),
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 (FP64 PCG scalars and solution)",
+        "data": "synthetic (seeded dam-break fill, no dataset)",
+        "config": {"workload": WORKLOAD, "grid": [res, res, res], "transfer": "APIC",
+                   "particles": int(np_mean), "dt": dt, "pcg_tol": "1e-6 relative L2",
+                   "obstacles": "moving sphere r=0.15, disc source r=4 cells, 8^3 sink box",
+                   "parallelism": f"replicas x{world}", "l2": "state 8.6 GB > L2; no flush needed",
+                   "warm_start": "zero"},
+        "particle_steps_per_s": round(np_mean * value, 1),
+        "pcg_iterations_mean": round(its, 2),
+        "stage_ms": {k: round(mean(k), 3) for k in ("ms_simulate_particles", "ms_p2g", "ms_p2g_kernel", "ms_prep",
+                                                   "ms_pcg_setup", "ms_solve", "ms_extrapolate", "ms_g2p")},
+        "pcg_ms_per_iteration": round(pcg_ms_per_it, 4),
+        "step_roofline": {"bytes": step_bytes, "achieved_gbs": round(step_bytes / (ms_step / 1e3) / 1e9, 1),
+                          "frac": round(step_bytes / (ms_step / 1e3) / 1e9 / peak, 4)},
+        "roofline": {"kernel": f"k_{dominant}", "bound": "hbm", "achieved": round(dk["gbs"], 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(dk["frac"], 4), "traffic": None,
+                     "peak_source": peak_kind,
+                     "all": {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
+                             for k, v in kernels.items()}},
+        "clocks": clocks,
+        "e2e": {"value": round(world * e2e_steps / (e2e_ms / 1000.0), 4), "unit": "steps/s",
+                "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps,
+                "steps": e2e_steps, "path": "fsim_step + fsim_fill_gfx(pinned host) per step"},
+        "gpu_launches": int(sum(s.kernel_launches for s in stats)),
+    }
+    sim.close()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(res, dt)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- CPU leg
+def cpu_baseline(res: int, dt: float, steps: int = 1, warm: int = 0):
+    """The reference's algorithm (FP64 oracle, all host threads) on the same workload."""
+    from oracle import oracle as O
+
+    O.build_port()
+    grid, pos = workload_scene(res)
+    h = grid.h
+    p = O.make_params(res, transfer=O.APIC, tol=1e-6, max_iters=2000, spawning=True, despawning=True)
+    o = O.Oracle(p, pos.astype(np.float64), lib="port")
+    del pos
+    cores = os.cpu_count() or 1
+    o.set_threads(cores)
+    t = 0.0
+    times = []
+    its = []
+    for k in range(warm + steps):
+        x = 0.5 + 0.1 * math.sin(math.pi * t)
+        xp = 0.5 + 0.1 * math.sin(math.pi * (t - dt))
+        o.set_obstacles([
+            O.obstacle(O.OBS_SPHERE, (x, 0.6, 0.5), r=0.15, prev_pos=(xp, 0.6, 0.5), speed=((x - xp) / dt, 0, 0)),
+            O.obstacle(O.OBS_DISC_SOURCE, (0.5, 0.95, 0.5), r=4 * h, spawn_speed=-1.0),
+            O.obstacle(O.OBS_BOX_SINK, (4 * h, 4 * h, 4 * h), size=(8 * h, 8 * h, 8 * h))])
+        t0 = time.perf_counter()
+        its.append(o.step(dt))
+        t1 = time.perf_counter()
+        if k >= warm:
+            times.append(t1 - t0)
+        t += dt
+    n = o.n
+    o.close()
+    sec = sum(times) / len(times)
+    return {"value": round(1.0 / sec, 5), "unit": "steps/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} full step(s) of {WORKLOAD} ({n} particles) after {warm} warm-up, "
+                      f"FP64 oracle, OpenMP x{cores}, MIC(0) PCG iterations {its[warm:]}",
+            "seconds_per_step": round(sec, 3)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if rank != 0:
+        return
+    res = args.res
+    dt = 1.0 / 480.0 if res == 256 else 1.0 / (480.0 * res / 256.0)
+    steps = max(1, min(args.steps, 2))
+    cb = cpu_baseline(res, dt, steps=steps, warm=1 if args.warmup > 0 else 0)
+    line = {
+        "impl": "reference",
+        "metric": "steps/s (256^3 APIC step, PCG to 1e-6 relative residual)",
+        "value": cb["value"],
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": steps,
+        "warmup": 1 if args.warmup > 0 else 0,
+        "ms_per_step": round(1000.0 * cb["seconds_per_step"], 1),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded dam-break fill, no dataset)",
+        "config": {"workload": WORKLOAD, "grid": [res, res, res], "transfer": "APIC",
+                   "note": f"reference algorithm on host cores; {steps} timed step(s) of the requested "
+                           f"{args.steps} (each takes tens of seconds)"},
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fsim", choices=["fsim", "reference"])
+    ap.add_argument("--res", type=int, default=256, help="grid resolution (256 = the benchmark workload)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--out-dir", default=os.path.join(ROOT, "gpurun_out"))
+    args = ap.parse_args()
+    os.makedirs(args.out_dir, exist_ok=True)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_fsim(args)
+
+
+if __name__ == "__main__":
+    main()

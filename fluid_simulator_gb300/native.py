@@ -1,0 +1,318 @@
+"""ctypes binding of the C ABI in include/fsim.h (libfsim.so, built in-tree).
+
+``Simulation`` is the Python-side mirror of the reference's per-step
+interface (Simulator + MacGrid + HashedParticles, src/Simulator/simulator):
+set particles and obstacles, step, read grid fields and particles back.  The
+library is the CUDA implementation; there is no CPU path here -- loading fails
+loudly when libfsim.so is missing or no GPU is visible.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfsim.so")
+
+PIC, FLIP, APIC = 0, 1, 2
+WATER, AIR, SOLID = 0, 1, 2
+HOST, DEVICE = 0, 1
+OBS_SPHERE, OBS_BOX, OBS_SOURCE, OBS_SINK, OBS_DISC_SOURCE, OBS_BOX_SINK = range(6)
+TOL_ABS_MAX, TOL_REL_L2 = 0, 1
+PREC_MIXED, PREC_FP32, PREC_FP64 = 0, 1, 2
+WARM_ZERO, WARM_PREVIOUS, WARM_GUESS = 0, 1, 2
+(STAGE_SPAWN, STAGE_ADVECT, STAGE_PUSH_APART, STAGE_PUSH_OUT, STAGE_STOP, STAGE_P2G, STAGE_MARK,
+ STAGE_OBSTACLES, STAGE_WALLS, STAGE_POST_P2G, STAGE_SOLVE, STAGE_EXTRAPOLATE, STAGE_G2P) = range(13)
+(F_FLAGS, F_AVGPNUM, F_VX, F_VY, F_VZ, F_V2X, F_V2Y, F_V2Z, F_PRESSURE, F_COUNT,
+ F_DIVERGENCE) = range(11)
+
+ERRORS = {0: "OK", -1: "INVALID", -2: "OOM", -3: "CUDA", -4: "NOT_CONVERGED", -5: "NAN",
+          -6: "TIMEOUT", -7: "UNSUPPORTED", -8: "STATE"}
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("dims", C.c_double * 3), ("resolution", C.c_double), ("two_d", C.c_int)]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("transfer", C.c_int), ("flip_ratio", C.c_float), ("gravity", C.c_float),
+        ("gravity_enabled", C.c_int), ("push_apart_enabled", C.c_int), ("spawning_enabled", C.c_int),
+        ("despawning_enabled", C.c_int), ("stop_particles", C.c_int), ("top_solid", C.c_int),
+        ("pressure_enabled", C.c_int), ("pressure_k", C.c_double), ("average_pressure", C.c_double),
+        ("max_iters", C.c_int), ("fluid_density", C.c_double), ("residual_tol", C.c_double),
+        ("tol_mode", C.c_int), ("particle_r", C.c_double), ("precision", C.c_int),
+        ("warm_start", C.c_int), ("track_ids", C.c_int), ("timing", C.c_int), ("reserved", C.c_int * 7),
+    ]
+
+
+class Obstacle(C.Structure):
+    _fields_ = [
+        ("type", C.c_int), ("pos", C.c_double * 3), ("prev_pos", C.c_double * 3),
+        ("speed", C.c_double * 3), ("r", C.c_double), ("size", C.c_double * 3),
+        ("spawn_rate", C.c_double), ("spawn_speed", C.c_double), ("last_spawn_fraction", C.c_double),
+    ]
+
+
+class ParticleGfx(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("v", C.c_float), ("density", C.c_float)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [
+        ("pcg_iterations", C.c_int), ("converged", C.c_int), ("num_particles", C.c_int),
+        ("num_fluid_cells", C.c_int), ("residual_max", C.c_double), ("residual_rel", C.c_double),
+        ("rhs_norm", C.c_double), ("guess_used", C.c_int), ("reliable_updates", C.c_int),
+        ("ms_simulate_particles", C.c_float), ("ms_push_apart", C.c_float), ("ms_push_out", C.c_float),
+        ("ms_p2g", C.c_float), ("ms_prep", C.c_float), ("ms_solve", C.c_float),
+        ("ms_extrapolate", C.c_float), ("ms_g2p", C.c_float), ("ms_total", C.c_float),
+        ("ms_p2g_kernel", C.c_float), ("ms_g2p_kernel", C.c_float), ("ms_pcg_setup", C.c_float),
+        ("kernel_launches", C.c_int), ("num_active_bricks", C.c_int), ("reserved", C.c_int * 3),
+    ]
+
+
+# exported symbols, in the order include/fsim.h declares them
+EXPORTS = [
+    "fsim_create", "fsim_destroy", "fsim_set_params", "fsim_get_params", "fsim_grid_info",
+    "fsim_last_error", "fsim_stream", "fsim_synchronize", "fsim_set_particles", "fsim_add_particles",
+    "fsim_get_particles", "fsim_num_particles", "fsim_set_obstacles", "fsim_get_obstacles",
+    "fsim_step", "fsim_stage", "fsim_get_grid", "fsim_set_grid", "fsim_fill_gfx",
+    "fsim_set_pressure_guess", "fsim_solve_pressure",
+]
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load libfsim.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: run `python __graft_entry__.py build` first")
+    lib = C.CDLL(path)
+    P, fp, dp, i64 = C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_double), C.c_int64
+    sig = {
+        "fsim_create": (C.c_int, [C.POINTER(GridDesc), C.POINTER(Params), C.POINTER(P)]),
+        "fsim_destroy": (C.c_int, [P]),
+        "fsim_set_params": (C.c_int, [P, C.POINTER(Params)]),
+        "fsim_get_params": (C.c_int, [P, C.POINTER(Params)]),
+        "fsim_grid_info": (C.c_int, [P, C.POINTER(C.c_int), dp, dp]),
+        "fsim_last_error": (C.c_char_p, [P]),
+        "fsim_stream": (P, [P]),
+        "fsim_synchronize": (C.c_int, [P]),
+        "fsim_set_particles": (C.c_int, [P, P, P, P, i64, C.c_int]),
+        "fsim_add_particles": (C.c_int, [P, P, P, P, i64, C.c_int]),
+        "fsim_get_particles": (C.c_int, [P, P, P, P, i64, C.POINTER(i64), C.c_int]),
+        "fsim_num_particles": (C.c_int, [P, C.POINTER(i64)]),
+        "fsim_set_obstacles": (C.c_int, [P, C.POINTER(Obstacle), C.c_int]),
+        "fsim_get_obstacles": (C.c_int, [P, C.POINTER(Obstacle), C.c_int, C.POINTER(C.c_int)]),
+        "fsim_step": (C.c_int, [P, C.c_double, C.POINTER(StepStats)]),
+        "fsim_stage": (C.c_int, [P, C.c_int, C.c_double, C.POINTER(StepStats)]),
+        "fsim_get_grid": (C.c_int, [P, C.c_int, P, C.c_int]),
+        "fsim_set_grid": (C.c_int, [P, C.c_int, P, C.c_int]),
+        "fsim_fill_gfx": (C.c_int, [P, C.POINTER(ParticleGfx), i64, C.POINTER(i64), C.c_int]),
+        "fsim_set_pressure_guess": (C.c_int, [P, fp, C.c_int]),
+        "fsim_solve_pressure": (C.c_int, [P, dp, C.c_double, C.c_int, C.c_int, C.c_double, C.c_int, dp,
+                                          C.POINTER(StepStats)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class FsimError(RuntimeError):
+    pass
+
+
+def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: float = 0.95,
+                   gravity: float = -9.81, max_iters: int = 200, tol: float = 1e-6,
+                   tol_mode: int = TOL_ABS_MAX, precision: int = PREC_MIXED, warm_start: int = WARM_ZERO,
+                   top_solid: bool = True, particle_r: float | None = None, spawning: bool = False,
+                   despawning: bool = False, stop_particles: bool = False, gravity_enabled: bool = True,
+                   pressure_enabled: bool = False, pressure_k: float = 2.0, average_pressure: float = 2.0,
+                   fluid_density: float = 1.0, timing: bool = False) -> Params:
+    """Parameters of the dam-break workloads (reference parameter names in fsim.h)."""
+    p = Params()
+    p.transfer = transfer
+    p.flip_ratio = flip_ratio
+    p.gravity = gravity
+    p.gravity_enabled = int(gravity_enabled)
+    p.push_apart_enabled = 0
+    p.spawning_enabled = int(spawning)
+    p.despawning_enabled = int(despawning)
+    p.stop_particles = int(stop_particles)
+    p.top_solid = int(top_solid)
+    p.pressure_enabled = int(pressure_enabled)
+    p.pressure_k = pressure_k
+    p.average_pressure = average_pressure
+    p.max_iters = max_iters
+    p.fluid_density = fluid_density
+    p.residual_tol = tol
+    p.tol_mode = tol_mode
+    h = 1.0 / float(np.float32(resolution))
+    p.particle_r = h / 4.0 if particle_r is None else particle_r
+    p.precision = precision
+    p.warm_start = warm_start
+    p.track_ids = 0
+    p.timing = int(timing)
+    return p
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class Simulation:
+    """One simulation context on the current CUDA device."""
+
+    def __init__(self, resolution: float, params: Params, *, dims=(1.0, 1.0, 1.0), track_ids: bool = False):
+        self.lib = load_library()
+        g = GridDesc()
+        g.dims[:] = list(dims)
+        g.resolution = resolution
+        g.two_d = 0
+        params.track_ids = int(track_ids)
+        self.params = params
+        self.ctx = C.c_void_p()
+        rc = self.lib.fsim_create(C.byref(g), C.byref(params), C.byref(self.ctx))
+        if rc != 0:
+            raise FsimError(f"fsim_create failed: {ERRORS.get(rc, rc)}")
+        n3 = (C.c_int * 3)()
+        h3 = (C.c_double * 3)()
+        d3 = (C.c_double * 3)()
+        self.lib.fsim_grid_info(self.ctx, n3, h3, d3)
+        self.shape = (n3[0], n3[1], n3[2])
+        self.h = h3[0]
+        self.dims = (d3[0], d3[1], d3[2])
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self.lib.fsim_last_error(self.ctx).decode()
+            raise FsimError(f"{what} failed: {ERRORS.get(rc, rc)}: {msg}")
+
+    def close(self):
+        if self.ctx:
+            self.lib.fsim_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params: Params):
+        params.track_ids = self.params.track_ids
+        self._check(self.lib.fsim_set_params(self.ctx, C.byref(params)), "fsim_set_params")
+        self.params = params
+
+    @property
+    def n(self) -> int:
+        n = C.c_int64()
+        self.lib.fsim_num_particles(self.ctx, C.byref(n))
+        return n.value
+
+    def set_particles(self, pos, vel=None, c=None):
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        vel = None if vel is None else np.ascontiguousarray(vel, np.float32).reshape(-1, 3)
+        c = None if c is None else np.ascontiguousarray(c, np.float32).reshape(-1, 9)
+        self._check(self.lib.fsim_set_particles(self.ctx, _ptr(pos), _ptr(vel), _ptr(c), pos.shape[0], HOST),
+                    "fsim_set_particles")
+
+    def add_particles(self, pos, vel=None, c=None):
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        vel = None if vel is None else np.ascontiguousarray(vel, np.float32).reshape(-1, 3)
+        c = None if c is None else np.ascontiguousarray(c, np.float32).reshape(-1, 9)
+        self._check(self.lib.fsim_add_particles(self.ctx, _ptr(pos), _ptr(vel), _ptr(c), pos.shape[0], HOST),
+                    "fsim_add_particles")
+
+    def particles(self):
+        n = self.n
+        pos = np.empty((n, 3), np.float32)
+        vel = np.empty((n, 3), np.float32)
+        c = np.empty((n, 3, 3), np.float32)
+        got = C.c_int64()
+        self._check(self.lib.fsim_get_particles(self.ctx, _ptr(pos), _ptr(vel), _ptr(c), n, C.byref(got), HOST),
+                    "fsim_get_particles")
+        return pos, vel, c
+
+    def set_obstacles(self, obstacles):
+        arr = (Obstacle * max(1, len(obstacles)))()
+        for i, o in enumerate(obstacles):
+            arr[i] = o
+        self._check(self.lib.fsim_set_obstacles(self.ctx, arr, len(obstacles)), "fsim_set_obstacles")
+
+    def obstacles(self):
+        arr = (Obstacle * 64)()
+        n = C.c_int()
+        self._check(self.lib.fsim_get_obstacles(self.ctx, arr, 64, C.byref(n)), "fsim_get_obstacles")
+        return [arr[i] for i in range(min(n.value, 64))]
+
+    def step(self, dt: float) -> StepStats:
+        st = StepStats()
+        self._check(self.lib.fsim_step(self.ctx, dt, C.byref(st)), "fsim_step")
+        return st
+
+    def stage(self, stage: int, dt: float) -> StepStats:
+        st = StepStats()
+        self._check(self.lib.fsim_stage(self.ctx, stage, dt, C.byref(st)), f"fsim_stage({stage})")
+        return st
+
+    def grid(self, field: int) -> np.ndarray:
+        dtype = {F_FLAGS: np.uint8, F_COUNT: np.int32}.get(field, np.float32)
+        out = np.empty(self.shape, dtype)
+        self._check(self.lib.fsim_get_grid(self.ctx, field, _ptr(out), HOST), "fsim_get_grid")
+        return out
+
+    def set_grid(self, field: int, values):
+        dtype = np.uint8 if field == F_FLAGS else np.float32
+        a = np.ascontiguousarray(values, dtype).reshape(self.shape)
+        self._check(self.lib.fsim_set_grid(self.ctx, field, _ptr(a), HOST), "fsim_set_grid")
+
+    def gfx(self) -> np.ndarray:
+        n = self.n
+        arr = (ParticleGfx * max(1, n))()
+        got = C.c_int64()
+        self._check(self.lib.fsim_fill_gfx(self.ctx, arr, n, C.byref(got), HOST), "fsim_fill_gfx")
+        out = np.frombuffer(arr, dtype=np.float32, count=5 * n).reshape(n, 5)
+        return out.copy()
+
+    def set_pressure_guess(self, p):
+        a = np.ascontiguousarray(p, np.float32).reshape(self.shape)
+        self._check(self.lib.fsim_set_pressure_guess(self.ctx, a.ctypes.data_as(C.POINTER(C.c_float)), HOST),
+                    "fsim_set_pressure_guess")
+
+    def solve_pressure(self, rhs, dt: float, *, precision: int = PREC_MIXED, tol_mode: int = TOL_REL_L2,
+                       tol: float = 1e-6, max_iters: int = 2000):
+        b = np.ascontiguousarray(rhs, np.float64).reshape(self.shape)
+        p = np.empty(self.shape, np.float64)
+        st = StepStats()
+        self._check(self.lib.fsim_solve_pressure(self.ctx, b.ctypes.data_as(C.POINTER(C.c_double)), dt,
+                                                 precision, tol_mode, tol, max_iters,
+                                                 p.ctypes.data_as(C.POINTER(C.c_double)), C.byref(st)),
+                    "fsim_solve_pressure")
+        return p, st
+
+    def synchronize(self):
+        self._check(self.lib.fsim_synchronize(self.ctx), "fsim_synchronize")
+
+
+def obstacle(kind: int, pos, *, r: float = 0.0, size=(0, 0, 0), speed=(0, 0, 0), prev_pos=None,
+             spawn_rate: float = 0.0, spawn_speed: float = 0.0, frac: float = 0.0) -> Obstacle:
+    o = Obstacle()
+    o.type = kind
+    o.pos[:] = list(pos)
+    o.prev_pos[:] = list(pos if prev_pos is None else prev_pos)
+    o.speed[:] = list(speed)
+    o.r = r
+    o.size[:] = list(size)
+    o.spawn_rate = spawn_rate
+    o.spawn_speed = spawn_speed
+    o.last_spawn_fraction = frac
+    return o

@@ -1,0 +1,273 @@
+/*
+ * fsim.h -- C ABI of the GB300 (sm_103a) fluid-simulation step library.
+ *
+ * One fsim_ctx owns a MAC grid, a particle set, the obstacle list and one CUDA
+ * stream on the current device.  It replaces the per-step path of the
+ * reference simulator (dkiovics/fluid_simulator, src/Simulator/simulator):
+ * Simulator::simulate (simulator.cpp:51-100) and the MacGrid /
+ * BridsonSolverGrid / HashedParticles state it runs on.  All calls are
+ * single-caller per context and stream-ordered; every function returns 0 or a
+ * negative FSIM_E_* code, and fsim_last_error() describes the last failure.
+ * No C++ exception crosses this boundary.
+ *
+ * Conventions
+ *   * Host arrays are FP32 AoS per particle: pos[3n], vel[3n], c[9n] where
+ *     c[9i + 3a + b] is component b of the APIC vector c[a] of particle i (the
+ *     reference's Particle::c, particle.h:8-12).
+ *   * Grid fields are exchanged in the reference's cell order, x-major with z
+ *     fastest: index (x*ny + y)*nz + z (MacGrid::cell, macGrid.h:91-93).  Face
+ *     field a of cell (x,y,z) is the face on the +a side of that cell
+ *     (MacGridCell::faces, macGrid.cpp:25-27).
+ *   * `where` selects host (FSIM_HOST) or device (FSIM_DEVICE) memory for the
+ *     caller's buffer; device buffers are only borrowed for the duration of the
+ *     call (the copy is stream-ordered and complete when the call returns).
+ */
+#ifndef FSIM_H
+#define FSIM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FSIM_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define FSIM_OK 0
+#define FSIM_E_INVALID (-1)       /* bad argument or unsupported combination */
+#define FSIM_E_OOM (-2)           /* device or host allocation failed */
+#define FSIM_E_CUDA (-3)          /* CUDA runtime/driver error */
+#define FSIM_E_NOT_CONVERGED (-4) /* reserved: the step itself reports convergence in stats */
+#define FSIM_E_NAN (-5)           /* non-finite solver scalar */
+#define FSIM_E_TIMEOUT (-6)       /* a bounded device-side wait gave up */
+#define FSIM_E_UNSUPPORTED (-7)   /* feature not built (see fsim_last_error) */
+#define FSIM_E_STATE (-8)         /* call out of order (e.g. G2P before P2G) */
+
+/* ---- enums ------------------------------------------------------------- */
+enum fsim_transfer { FSIM_PIC = 0, FSIM_FLIP = 1, FSIM_APIC = 2 }; /* Simulator::P2G2PType */
+enum fsim_cell { FSIM_WATER = 0, FSIM_AIR = 1, FSIM_SOLID = 2 };   /* MacGridCell::CellType */
+enum fsim_where { FSIM_HOST = 0, FSIM_DEVICE = 1 };
+
+enum fsim_obstacle_type {
+    FSIM_OBS_SPHERE = 0,      /* SphericalObstacle (obstacles.hpp:36-44) */
+    FSIM_OBS_BOX = 1,         /* RectengularObstacle (obstacles.hpp:26-34) */
+    FSIM_OBS_SOURCE = 2,      /* SphericalParticleSource (obstacles.hpp:46-57) */
+    FSIM_OBS_SINK = 3,        /* SphericalParticleSink (obstacles.hpp:59-65) */
+    FSIM_OBS_DISC_SOURCE = 4, /* extension: horizontal disc emitting 8 jittered particles
+                                 per covered cell per step (no reference counterpart) */
+    FSIM_OBS_BOX_SINK = 5     /* extension: axis-aligned box deleting particles */
+};
+
+/* Convergence test of the pressure solve. */
+enum fsim_tol_mode {
+    FSIM_TOL_ABS_MAX = 0, /* max_i |r_i| < tol: the reference's test (bridsonSolverGrid.cpp:276-281) */
+    FSIM_TOL_REL_L2 = 1   /* ||r||_2 <= tol * ||b||_2 */
+};
+
+/* Arithmetic of the pressure solve. */
+enum fsim_precision {
+    FSIM_PREC_MIXED = 0, /* FP32 vectors/stencils/preconditioner, FP64 dots and scalars,
+                            FP64 solution with FP64 true-residual replacement */
+    FSIM_PREC_FP32 = 1,  /* as MIXED but the solution and residual stay FP32 */
+    FSIM_PREC_FP64 = 2   /* all-FP64 PCG (precision-study oracle on the device) */
+};
+
+/* Initial guess of the pressure solve. */
+enum fsim_warm_start {
+    FSIM_WARM_ZERO = 0,     /* p0 = 0, as the reference */
+    FSIM_WARM_PREVIOUS = 1, /* previous step's pressure */
+    FSIM_WARM_GUESS = 2     /* fsim_set_pressure_guess, falling back to the previous step's
+                               pressure when the guess has the larger residual */
+};
+
+/* Step stages, in the order Simulator::simulate runs them (simulator.cpp:51-100). */
+enum fsim_stage {
+    FSIM_STAGE_SPAWN = 0,
+    FSIM_STAGE_ADVECT = 1,
+    FSIM_STAGE_PUSH_APART = 2, /* not built: returns FSIM_E_UNSUPPORTED */
+    FSIM_STAGE_PUSH_OUT = 3,
+    FSIM_STAGE_STOP = 4,
+    FSIM_STAGE_P2G = 5,       /* sort by cell + resetGridValues + p2gTransfer + marking */
+    FSIM_STAGE_MARK = 6,      /* fused into FSIM_STAGE_P2G (no-op) */
+    FSIM_STAGE_OBSTACLES = 7,
+    FSIM_STAGE_WALLS = 8,
+    FSIM_STAGE_POST_P2G = 9,
+    FSIM_STAGE_SOLVE = 10,
+    FSIM_STAGE_EXTRAPOLATE = 11,
+    FSIM_STAGE_G2P = 12,
+    FSIM_NUM_STAGES = 13
+};
+
+/* Grid fields for fsim_get_grid / fsim_set_grid. */
+enum fsim_field {
+    FSIM_F_FLAGS = 0,   /* uint8 fsim_cell */
+    FSIM_F_AVGPNUM = 1, /* float: particle density (MacGridCell::avgPNum) */
+    FSIM_F_VX = 2, FSIM_F_VY = 3, FSIM_F_VZ = 4,    /* float face v (after P2G/obstacles/walls) */
+    FSIM_F_V2X = 5, FSIM_F_V2Y = 6, FSIM_F_V2Z = 7, /* float face v2 */
+    FSIM_F_PRESSURE = 8, /* float: last solved pressure, 0 outside fluid */
+    FSIM_F_COUNT = 9,    /* int32: particles per cell from the last sort */
+    FSIM_F_DIVERGENCE = 10 /* float: pressure right-hand side of the last solve */
+};
+
+/* ---- structs ----------------------------------------------------------- */
+
+/* MacGrid(targetDimensions, resolution, twoD) (macGrid.h:28). */
+typedef struct fsim_grid_desc {
+    double dims[3];    /* target dimensions */
+    double resolution; /* cells per unit length (rounded to float as BridsonSolverGrid does) */
+    int two_d;         /* must be 0: 2D mode is not built */
+} fsim_grid_desc;
+
+/* Simulator::SimulatorConfig (simulator.h:30-39) + MacGrid public fields
+ * (macGrid.h:173-179) + the particle radius + solver controls. */
+typedef struct fsim_params {
+    int transfer;           /* fsim_transfer */
+    float flip_ratio;
+    float gravity;          /* signed, added to v_y * dt */
+    int gravity_enabled;
+    int push_apart_enabled; /* must be 0 (not built) */
+    int spawning_enabled;
+    int despawning_enabled;
+    int stop_particles;
+    int top_solid;          /* isTopOfContainerSolid */
+    int pressure_enabled;   /* density-correction term in the rhs */
+    double pressure_k;
+    double average_pressure;
+    int max_iters;          /* incompressibilityMaxIterationCount */
+    double fluid_density;
+    double residual_tol;
+    int tol_mode;           /* fsim_tol_mode */
+    double particle_r;
+    int precision;          /* fsim_precision */
+    int warm_start;         /* fsim_warm_start */
+    int track_ids;          /* keep a stable id per particle (fsim_get_particles in id order) */
+    int timing;             /* record per-stage CUDA-event times into fsim_step_stats */
+    int reserved[7];
+} fsim_params;
+
+/* Obstacle (obstacles.hpp:7-65), speed set by the caller as (pos-prevPos)/dt. */
+typedef struct fsim_obstacle {
+    int type; /* fsim_obstacle_type */
+    double pos[3];
+    double prev_pos[3];
+    double speed[3];
+    double r;       /* spheres, sources, sinks, disc sources */
+    double size[3]; /* boxes and box sinks */
+    double spawn_rate;  /* sources: particles per second */
+    double spawn_speed; /* sources: speed along the normal; disc sources: v_y */
+    double last_spawn_fraction;
+} fsim_obstacle;
+
+/* SimulationManager::ParticleGfxData (simulationManager.h:74-78). */
+typedef struct fsim_particle_gfx {
+    float pos[3];
+    float v;       /* |velocity| */
+    float density; /* trilinear avgPNum at the particle */
+} fsim_particle_gfx;
+
+/* Per-step statistics.  stage_ms follows the reference's getStepDuration keys
+ * (simulator.cpp:33-40), measured by CUDA events when fsim_params.timing != 0. */
+typedef struct fsim_step_stats {
+    int pcg_iterations;  /* "Incompressibility it count" */
+    int converged;
+    int num_particles;
+    int num_fluid_cells;
+    double residual_max;  /* true residual after the solve, max norm */
+    double residual_rel;  /* true residual after the solve, ||r||/||b|| */
+    double rhs_norm;
+    int guess_used;       /* FSIM_WARM_* actually used */
+    int reliable_updates;
+    float ms_simulate_particles;  /* "SimulateParticles": spawn + advect + push-out */
+    float ms_push_apart;          /* "PushParticlesApart" */
+    float ms_push_out;            /* "PushParticlesOutOfObstacles" (fused into advect: 0) */
+    float ms_p2g;                 /* "P2GTransfer": sort + P2G + marking */
+    float ms_prep;                /* "IncompressibilityPrep": obstacles, walls, v2 */
+    float ms_solve;               /* "Incompressibility" */
+    float ms_extrapolate;         /* "VelocityExtrapolation" */
+    float ms_g2p;                 /* "G2PTransfer" */
+    float ms_total;
+    float ms_p2g_kernel;          /* the P2G tile kernel alone */
+    float ms_g2p_kernel;          /* the G2P tile kernel alone */
+    float ms_pcg_setup;           /* solve setup: codes, rhs, bricks, first residual */
+    int kernel_launches;          /* CUDA kernels this call launched */
+    int num_active_bricks;        /* pressure-solve bricks holding fluid */
+    int reserved[3];
+} fsim_step_stats;
+
+typedef struct fsim_ctx fsim_ctx;
+
+/* ---- lifecycle --------------------------------------------------------- */
+
+/* Create a context on the current CUDA device.  Replaces the construction in
+ * SimulationManager::SimulationManager (simulationManager.cpp:10-29):
+ * BridsonSolverGrid + HashedParticles + Simulator. */
+int fsim_create(const fsim_grid_desc *grid, const fsim_params *params, fsim_ctx **out);
+int fsim_destroy(fsim_ctx *ctx);
+/* Replaces the per-step parameter copy in SimulationManager::simulationThreadWorker
+ * (simulationManager.cpp:184-199). */
+int fsim_set_params(fsim_ctx *ctx, const fsim_params *params);
+int fsim_get_params(fsim_ctx *ctx, fsim_params *out);
+/* gridSize (cells), cellD and dimensions of MacGrid (macGrid.h:168-171). */
+int fsim_grid_info(fsim_ctx *ctx, int *n3, double *h3, double *dims3);
+const char *fsim_last_error(fsim_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t). */
+void *fsim_stream(fsim_ctx *ctx);
+int fsim_synchronize(fsim_ctx *ctx);
+
+/* ---- particles (HashedParticles, hashedParticles.h:30-177) -------------- */
+
+/* Replace all particles (HashedParticles ctor / setParticleNum + getParticleAt writes).
+ * vel and c may be NULL (zero). */
+int fsim_set_particles(fsim_ctx *ctx, const float *pos, const float *vel, const float *c,
+                       int64_t n, int where);
+/* Append particles (HashedParticles::addParticles, hashedParticles.cpp:153-156). */
+int fsim_add_particles(fsim_ctx *ctx, const float *pos, const float *vel, const float *c,
+                       int64_t n, int where);
+/* Copy particles out (getParticleAt / forEach).  With track_ids the order is by
+ * particle id, i.e. the order the reference's vector would have; otherwise the
+ * device order.  *n receives the count; cap bounds the copy. */
+int fsim_get_particles(fsim_ctx *ctx, float *pos, float *vel, float *c, int64_t cap, int64_t *n,
+                       int where);
+int fsim_num_particles(fsim_ctx *ctx, int64_t *n);
+
+/* ---- obstacles (Simulator::obstacles, simulator.h:74) ------------------- */
+int fsim_set_obstacles(fsim_ctx *ctx, const fsim_obstacle *obs, int n);
+/* Read back (sources carry last_spawn_fraction between steps). */
+int fsim_get_obstacles(fsim_ctx *ctx, fsim_obstacle *obs, int cap, int *n);
+
+/* ---- stepping ---------------------------------------------------------- */
+
+/* One Simulator::simulate(dt) (simulator.cpp:51-100).  stats may be NULL. */
+int fsim_step(fsim_ctx *ctx, double dt, fsim_step_stats *stats);
+/* One stage of the step, for stage-by-stage checking against the reference's
+ * member functions (fsim_stage enum). */
+int fsim_stage(fsim_ctx *ctx, int stage, double dt, fsim_step_stats *stats);
+
+/* ---- grid state (MacGrid::cell / getCellAt, macGrid.h:48-93) ------------ */
+int fsim_get_grid(fsim_ctx *ctx, int field, void *out, int where);
+/* Overwrite a grid field (FLAGS, AVGPNUM, V*, V2*, PRESSURE). */
+int fsim_set_grid(fsim_ctx *ctx, int field, const void *in, int where);
+
+/* ---- renderer hand-off (SimulationManager::getParticleGfxData,
+ *      simulationManager.cpp:218-231) ------------------------------------- */
+int fsim_fill_gfx(fsim_ctx *ctx, fsim_particle_gfx *out, int64_t cap, int64_t *n, int where);
+
+/* ---- pressure warm start ----------------------------------------------- */
+/* Initial guess for the next solve (FP32, reference cell order); used when
+ * params.warm_start == FSIM_WARM_GUESS.  No reference counterpart: the
+ * reference always starts PCG from zero (bridsonSolverGrid.cpp:249). */
+int fsim_set_pressure_guess(fsim_ctx *ctx, const float *p, int where);
+
+/* ---- pressure-only solve (precision study) ------------------------------ */
+/* Solve A p = rhs on the current cell flags, with the given precision and
+ * tolerance; rhs/out are FP64 in reference cell order (host).  Used to compare
+ * the solver variants on identical inputs. */
+int fsim_solve_pressure(fsim_ctx *ctx, const double *rhs, double dt, int precision, int tol_mode,
+                        double tol, int max_iters, double *p_out, fsim_step_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FSIM_H */

@@ -274,10 +274,37 @@ static inline d3 obs_speed(const oracle_obstacle *o) { d3 r = {o->speed[0], o->s
  * (util/random.h:23-25) on the C library's rand(). */
 static double rand_in(double lo, double hi) { return lo + (hi - lo) * ((double)rand() / RAND_MAX); }
 
+/* Disc source (extension): 8 particles per covered cell of the cell row at
+ * pos.y, one per 2x2x2 sub-cell with +-0.5 sub-cell jitter, velocity (0, speed, 0). */
+static void spawn_disc(sim *s, const oracle_obstacle *o) {
+    const double h = s->cd.x;
+    const int cy = (int)(o->pos[1] * s->cdi.y);
+    if (cy < 1 || cy >= s->ny - 1) return;
+    const double cx = o->pos[0] * s->cdi.x, cz = o->pos[2] * s->cdi.z, r = o->r * s->cdi.x;
+    for (int x = 1; x < s->nx - 1; x++)
+        for (int z = 1; z < s->nz - 1; z++) {
+            const double dx = x + 0.5 - cx, dz = z + 0.5 - cz;
+            if (dx * dx + dz * dz > r * r) continue;
+            for (int q = 0; q < 8; q++) {
+                const double sub[3] = {(q & 4) ? 0.75 : 0.25, (q & 2) ? 0.75 : 0.25, (q & 1) ? 0.75 : 0.25};
+                const double base[3] = {(double)x, (double)cy, (double)z};
+                int idx = s->n;
+                particles_resize(s, s->n + 1);
+                particle *p = &s->pt[idx];
+                double c[3];
+                for (int a = 0; a < 3; a++) c[a] = (base[a] + sub[a] + (rand_in(0.0, 1.0) - 0.5) * 0.5 * 0.999) * h;
+                p->pos.x = c[0]; p->pos.y = c[1]; p->pos.z = c[2];
+                p->v.x = 0.0; p->v.y = o->spawn_speed; p->v.z = 0.0;
+                memset(p->c, 0, sizeof(p->c));
+            }
+        }
+}
+
 static void stage_spawn(sim *s, double dt) {
     const double pr = s->p.particle_r;
     for (int k = 0; k < s->nobs; k++) {
         oracle_obstacle *o = &s->obs[k];
+        if (o->type == ORACLE_OBS_DISC_SOURCE) { spawn_disc(s, o); continue; }
         if (o->type != ORACLE_OBS_SOURCE) continue;
         double r = o->r + pr;
         double numd = o->spawn_rate * dt + o->last_spawn_fraction;
@@ -357,6 +384,16 @@ static void stage_advect(sim *s, double dt) {
             for (int k = 0; k < s->nobs; k++) {
                 const oracle_obstacle *o = &s->obs[k];
                 d3 op = obs_pos(o), os = obs_speed(o);
+                if (o->type == ORACLE_OBS_BOX_SINK) {
+                    if (despawn && fabs(q->pos.x - op.x) < o->size[0] * 0.5 &&
+                        fabs(q->pos.y - op.y) < o->size[1] * 0.5 && fabs(q->pos.z - op.z) < o->size[2] * 0.5) {
+#pragma omp critical(fsim_oracle_remove)
+                        remove[nremove++] = idx;
+                        collision = 0;
+                        break;
+                    }
+                    continue;
+                }
                 if (is_spherical(o->type)) {
                     int isSink = o->type == ORACLE_OBS_SINK;
                     double r = o->r + pr;

@@ -27,7 +27,7 @@ REF_LIB = os.path.join(HERE, "_ref", "libfsim_ref.so")
 
 PIC, FLIP, APIC = 0, 1, 2
 WATER, AIR, SOLID = 0, 1, 2
-OBS_SPHERE, OBS_BOX, OBS_SOURCE, OBS_SINK = 0, 1, 2, 3
+OBS_SPHERE, OBS_BOX, OBS_SOURCE, OBS_SINK, OBS_DISC_SOURCE, OBS_BOX_SINK = 0, 1, 2, 3, 4, 5
 
 (STAGE_SPAWN, STAGE_ADVECT, STAGE_PUSH_APART, STAGE_PUSH_OUT, STAGE_STOP, STAGE_P2G,
  STAGE_MARK, STAGE_OBSTACLES, STAGE_WALLS, STAGE_POST_P2G, STAGE_SOLVE,

@@ -36,7 +36,11 @@ enum oracle_obstacle_type {
     ORACLE_OBS_SPHERE = 0, /* SphericalObstacle (obstacles.hpp:36-44) */
     ORACLE_OBS_BOX = 1,    /* RectengularObstacle (obstacles.hpp:26-34) */
     ORACLE_OBS_SOURCE = 2, /* SphericalParticleSource (obstacles.hpp:46-57) */
-    ORACLE_OBS_SINK = 3    /* SphericalParticleSink (obstacles.hpp:59-65) */
+    ORACLE_OBS_SINK = 3,   /* SphericalParticleSink (obstacles.hpp:59-65) */
+    /* extensions of the 256^3 benchmark workload (no reference counterpart;
+     * the reference library ignores them) */
+    ORACLE_OBS_DISC_SOURCE = 4, /* horizontal disc: 8 jittered particles per covered cell per step */
+    ORACLE_OBS_BOX_SINK = 5     /* axis-aligned box deleting particles */
 };
 
 typedef struct oracle_params {

@@ -256,6 +256,7 @@ void oracle_set_obstacles(void* hv, int n, const oracle_obstacle* obs) {
     h->sim->obstacles.clear();
     for (int i = 0; i < n; i++) {
         const oracle_obstacle& o = obs[i];
+        if (o.type > ORACLE_OBS_SINK) continue;  // extensions have no reference counterpart
         const glm::dvec3 pos(o.pos[0], o.pos[1], o.pos[2]);
         obstacle::Obstacle* made = nullptr;
         switch (o.type) {
