@@ -52,8 +52,14 @@ __device__ __forceinline__ int code_nf(uint16_t c) { return __popc(c & 0x3F); }
 struct BrickGeo {
     GridGeom g;
     int nbx, nby, nbz;
-    long long off[6];  // +x, -x, +y, -y, +z, -z
+    long long sx, sy;  // strides of +x and +y (+z is 1)
 };
+
+// neighbour offset k: +x, -x, +y, -y, +z, -z (bit k of the fluid mask)
+__device__ __forceinline__ long long nb_off(const BrickGeo& B, int k) {
+    const long long st = (k >> 1) == 0 ? B.sx : ((k >> 1) == 1 ? B.sy : 1ll);
+    return (k & 1) ? -st : st;
+}
 
 __device__ __forceinline__ bool brick_cell(const BrickGeo& B, int b, int t, int& x, int& y, int& z,
                                            long long& c) {
@@ -67,21 +73,49 @@ __device__ __forceinline__ bool brick_cell(const BrickGeo& B, int b, int t, int&
 }
 
 __constant__ float c_fill[7][7];  // (1 + tau (nf - 1)) / ns
+__constant__ float c_rcp[7];      // 1 / ns (1 for ns = 0)
+
+// Per-thread sums.  GB300 runs FP64 at a small fraction of its FP32 rate, so
+// per-cell terms are summed in FP32 with compensation (Kahan), and only the
+// per-thread totals enter the FP64 block / grid reduction.
+template <typename T>
+struct Acc {
+    T s = 0;
+    __device__ __forceinline__ void add(T x) { s += x; }
+    __device__ __forceinline__ double value() const { return (double)s; }
+};
+template <>
+struct Acc<float> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+template <typename T>
+__device__ __forceinline__ T recip_ns(int ns);
+template <>
+__device__ __forceinline__ float recip_ns<float>(int ns) { return c_rcp[ns]; }
+template <>
+__device__ __forceinline__ double recip_ns<double>(int ns) { return ns > 0 ? 1.0 / ns : 1.0; }
 
 __device__ __forceinline__ float black_pivot_inv(const uint16_t* code, long long c, uint16_t cc,
-                                                 const long long* off) {
+                                                 const BrickGeo& B) {
     const int ns = code_ns(cc);
     if (ns == 0) return 1.f;
     float d = (float)ns;
 #pragma unroll
     for (int k = 0; k < 6; k++) {
         if ((cc >> k) & 1) {
-            const uint16_t cj = code[c + off[k]];
+            const uint16_t cj = code[c + nb_off(B, k)];
             d -= c_fill[code_nf(cj)][code_ns(cj)];
         }
     }
     if (d < SAFE * ns) d = (float)ns;
-    return 1.f / d;
+    return __frcp_rn(d);
 }
 
 // ---- setup: codes, rhs, initial guess, brick activity ----------------------
@@ -117,10 +151,9 @@ __global__ void k_setup(const SetupArgs a) {
     }
     uint16_t code = CODE_FLUID;
     int ns = 0;
-    const long long* off = a.B.off;
 #pragma unroll
     for (int k = 0; k < 6; k++) {
-        const uint8_t fn = a.flags[c + off[k]];
+        const uint8_t fn = a.flags[c + nb_off(a.B, k)];
         if (fn == C_WATER) code |= (uint16_t)(1u << k);
         if (fn != C_SOLID) ns++;
     }
@@ -131,8 +164,8 @@ __global__ void k_setup(const SetupArgs a) {
         bb = a.rhs_override[c];
     } else {
         const double sum = (double)a.v2[0][c] + (double)a.v2[1][c] + (double)a.v2[2][c] -
-                           (double)a.v2[0][c + off[1]] - (double)a.v2[1][c + off[3]] -
-                           (double)a.v2[2][c + off[5]];
+                           (double)a.v2[0][c - a.B.sx] - (double)a.v2[1][c - a.B.sy] -
+                           (double)a.v2[2][c - 1];
         double rhs = -a.inv_h * sum;
         if (a.pressure_enabled) rhs += ((double)a.avg[c] - a.avg_pressure) * a.pressure_k;
         bb = rhs * a.inv_scale;
@@ -200,7 +233,7 @@ struct Vecs {
 template <typename T>
 __global__ void __launch_bounds__(PCG_THREADS) k_residual(const PcgArgs a, Vecs<T> v, int first, int reset_x) {
     __shared__ double scratch[32 * 4];
-    T* r = v.r[a.st->bufsel & 1];
+    T* r = (a.st->bufsel & 1) ? v.r[1] : v.r[0];
     double acc[4] = {0.0, -1e300, 0.0, -1e300};  // rr, rmax, bb, bmax
     const int nact = *a.nactive;
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
@@ -213,7 +246,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_residual(const PcgArgs a, Vecs<
         double ap = (double)code_ns(cc) * phi[c];
 #pragma unroll
         for (int k = 0; k < 6; k++)
-            if ((cc >> k) & 1) ap -= phi[c + a.B.off[k]];
+            if ((cc >> k) & 1) ap -= phi[c + nb_off(a.B, k)];
         const double bc = a.b[c];
         const double rv = bc - ap;
         r[c] = (T)rv;
@@ -247,7 +280,7 @@ template <typename T>
 __global__ void __launch_bounds__(PCG_THREADS) k_black(const PcgArgs a, Vecs<T> v) {
     if (a.st->done) return;
     const int rc = a.st->bufsel & 1;
-    const T* r = v.r[rc];
+    const T* r = rc ? v.r[1] : v.r[0];
     const int nact = *a.nactive;
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int x, y, z;
@@ -256,15 +289,14 @@ __global__ void __launch_bounds__(PCG_THREADS) k_black(const PcgArgs a, Vecs<T> 
         if (((x + y + z) & 1) == 0) continue;
         const uint16_t cc = a.code[c];
         if (!(cc & CODE_FLUID)) continue;
-        double accd = (double)r[c];
+        T sum = r[c];
 #pragma unroll
         for (int k = 0; k < 6; k++)
             if ((cc >> k) & 1) {
-                const long long j = c + a.B.off[k];
-                const uint16_t cj = a.code[j];
-                accd += (double)r[j] / (double)code_ns(cj);
+                const long long j = c + nb_off(a.B, k);
+                sum += r[j] * recip_ns<T>(code_ns(a.code[j]));
             }
-        v.z[c] = (T)(accd * (double)black_pivot_inv(a.code, c, cc, a.B.off));
+        v.z[c] = sum * (T)black_pivot_inv(a.code, c, cc, a.B);
     }
 }
 
@@ -277,8 +309,8 @@ __global__ void __launch_bounds__(PCG_THREADS) k_red(const PcgArgs a, Vecs<T> v,
     __shared__ double scratch[32];
     if (a.st->done) return;
     const int rc = a.st->bufsel & 1;
-    const T* r = v.r[rc];
-    double acc[1] = {0.0};
+    const T* r = rc ? v.r[1] : v.r[0];
+    Acc<T> zr;
     const int nact = *a.nactive;
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int x, y, z;
@@ -286,22 +318,21 @@ __global__ void __launch_bounds__(PCG_THREADS) k_red(const PcgArgs a, Vecs<T> v,
         if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, z, c)) continue;
         const uint16_t cc = a.code[c];
         if (!(cc & CODE_FLUID)) continue;
-        const double rv = (double)r[c];
-        double zv;
+        const T rv = r[c];
+        T zv;
         if (((x + y + z) & 1) == 0) {
-            double s = rv;
+            T sum = rv;
 #pragma unroll
             for (int k = 0; k < 6; k++)
-                if ((cc >> k) & 1) s += (double)v.z[c + a.B.off[k]];
-            const int ns = code_ns(cc);
-            zv = s / (double)(ns > 0 ? ns : 1);
-            v.z[c] = (T)zv;
-            zv = (double)(T)zv;
+                if ((cc >> k) & 1) sum += v.z[c + nb_off(a.B, k)];
+            zv = sum * recip_ns<T>(code_ns(cc));
+            v.z[c] = zv;
         } else {
-            zv = (double)v.z[c];
+            zv = v.z[c];
         }
-        acc[0] += zv * rv;
+        zr.add(zv * rv);
     }
+    double acc[1] = {zr.value()};
     if (last_block_reduce<1>(acc, 0, a.partials, a.counter, scratch)) {
         if (threadIdx.x == 0) {
             PcgState* s = a.st;
@@ -333,9 +364,10 @@ __global__ void __launch_bounds__(PCG_THREADS) k_spmv(const PcgArgs a, Vecs<T> v
     if (a.st->done) return;
     const int sc = (a.st->bufsel >> 1) & 1;
     const double beta = a.st->beta;
-    const T* so = v.s[sc];
-    T* sn = v.s[1 - sc];
-    double acc[1] = {0.0};
+    const T* so = sc ? v.s[1] : v.s[0];
+    T* sn = sc ? v.s[0] : v.s[1];
+    Acc<T> sq;
+    const T betaT = (T)beta;
     const int nact = *a.nactive;
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int x, y, z;
@@ -343,18 +375,19 @@ __global__ void __launch_bounds__(PCG_THREADS) k_spmv(const PcgArgs a, Vecs<T> v
         if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, z, c)) continue;
         const uint16_t cc = a.code[c];
         if (!(cc & CODE_FLUID)) continue;
-        const T snc = v.z[c] + (T)beta * so[c];
+        const T snc = v.z[c] + betaT * so[c];
         T qv = (T)code_ns(cc) * snc;
 #pragma unroll
         for (int k = 0; k < 6; k++)
             if ((cc >> k) & 1) {
-                const long long j = c + a.B.off[k];
-                qv -= v.z[j] + (T)beta * so[j];
+                const long long j = c + nb_off(a.B, k);
+                qv -= v.z[j] + betaT * so[j];
             }
         sn[c] = snc;
         v.q[c] = qv;
-        acc[0] += (double)snc * (double)qv;
+        sq.add(snc * qv);
     }
+    double acc[1] = {sq.value()};
     if (last_block_reduce<1>(acc, 0, a.partials, a.counter, scratch)) {
         if (threadIdx.x == 0) {
             PcgState* s = a.st;
@@ -375,10 +408,11 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
     if (a.st->done) return;
     const int rc = a.st->bufsel & 1, sc = (a.st->bufsel >> 1) & 1;
     const T alpha = (T)a.st->alpha;
-    const T* ro = v.r[rc];
-    T* rn = v.r[1 - rc];
-    const T* s = v.s[sc];
-    double acc[2] = {0.0, -1e300};
+    const T* ro = rc ? v.r[1] : v.r[0];
+    T* rn = rc ? v.r[0] : v.r[1];
+    const T* s = sc ? v.s[1] : v.s[0];
+    Acc<T> rr;
+    T rmax = (T)0;
     const int nact = *a.nactive;
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int x, y, z;
@@ -389,20 +423,21 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
         v.x[c] += alpha * s[c];
         const T rv = ro[c] - alpha * v.q[c];
         rn[c] = rv;
-        acc[0] += (double)rv * (double)rv;
-        acc[1] = fmax(acc[1], fabs((double)rv));
+        rr.add(rv * rv);
+        rmax = fmax(rmax, fabs(rv));
         if ((x + y + z) & 1) {
             T sum = rv;
 #pragma unroll
             for (int k = 0; k < 6; k++)
                 if ((cc >> k) & 1) {
-                    const long long j = c + a.B.off[k];
+                    const long long j = c + nb_off(a.B, k);
                     const uint16_t cj = a.code[j];
-                    sum += (ro[j] - alpha * v.q[j]) / (T)code_ns(cj);
+                    sum += (ro[j] - alpha * v.q[j]) * recip_ns<T>(code_ns(cj));
                 }
-            v.z[c] = sum * (T)black_pivot_inv(a.code, c, cc, a.B.off);
+            v.z[c] = sum * (T)black_pivot_inv(a.code, c, cc, a.B);
         }
     }
+    double acc[2] = {rr.value(), (double)rmax};
     if (last_block_reduce<2>(acc, 0x2, a.partials, a.counter, scratch)) {
         if (threadIdx.x == 0) {
             PcgState* st = a.st;
@@ -473,6 +508,9 @@ int solver_alloc(fsim_ctx* ctx) {
     for (int nf = 0; nf < 7; nf++)
         for (int ns = 0; ns < 7; ns++) fill[nf][ns] = ns > 0 ? (1.f + TAU * (nf - 1)) / ns : 0.f;
     FSIM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_fill, fill, sizeof(fill)));
+    float rcp[7];
+    for (int ns = 0; ns < 7; ns++) rcp[ns] = ns > 0 ? 1.f / ns : 1.f;
+    FSIM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rcp, rcp, sizeof(rcp)));
     return FSIM_OK;
 }
 
@@ -581,8 +619,8 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     BrickGeo B;
     B.g = g;
     B.nbx = S.nbx; B.nby = S.nby; B.nbz = S.nbz;
-    const long long sx = (long long)g.pz * g.ny, sy = g.pz;
-    B.off[0] = sx; B.off[1] = -sx; B.off[2] = sy; B.off[3] = -sy; B.off[4] = 1; B.off[5] = -1;
+    B.sx = (long long)g.pz * g.ny;
+    B.sy = g.pz;
 
     FSIM_CUDA_TRY(ctx, cudaMemsetAsync(S.brick_flag, 0, S.nbricks, st));
     SetupArgs sa;
