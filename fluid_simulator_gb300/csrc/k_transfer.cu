@@ -361,6 +361,30 @@ void launch_p2g(fsim_ctx* ctx) {
         k_p2g<false><<<nb, P2G_THREADS, P2G_SMEM, ctx->stream>>>(a);
 }
 
+// P2G on caller-provided buffers (used by the allocation-free entry point in
+// fsim_static.cu); same kernel as launch_p2g.
+void launch_p2g_raw(ParticleBuf p, const uint32_t* perm, const int* cstart, const GridGeom& g, float* const u[3],
+                    uint8_t* flags, float* avg, bool apic, cudaStream_t stream) {
+    P2GArgs a;
+    a.p = p;
+    a.perm = perm;
+    a.cstart = cstart;
+    a.g = g;
+    for (int k = 0; k < 3; k++) a.u[k] = u[k];
+    a.flags = flags;
+    a.avg = avg;
+    a.ntx = ceil_div(g.nx, TX);
+    a.nty = ceil_div(g.ny, TY);
+    a.ntz = ceil_div(g.nz, TZ);
+    const int nb = a.ntx * a.nty * a.ntz;
+    cudaFuncSetAttribute(k_p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
+    cudaFuncSetAttribute(k_p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
+    if (apic)
+        k_p2g<true><<<nb, P2G_THREADS, P2G_SMEM, stream>>>(a);
+    else
+        k_p2g<false><<<nb, P2G_THREADS, P2G_SMEM, stream>>>(a);
+}
+
 // TMA descriptors of the six face arrays (v2 x/y/z, v x/y/z): 3D tensors
 // (z innermost, padded pitch pz), box BZ x BY x BX floats, zero fill outside.
 bool make_tensor_maps(fsim_ctx* ctx) {

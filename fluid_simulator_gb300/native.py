@@ -29,7 +29,7 @@ WARM_ZERO, WARM_PREVIOUS, WARM_GUESS = 0, 1, 2
  F_DIVERGENCE) = range(11)
 
 ERRORS = {0: "OK", -1: "INVALID", -2: "OOM", -3: "CUDA", -4: "NOT_CONVERGED", -5: "NAN",
-          -6: "TIMEOUT", -7: "UNSUPPORTED", -8: "STATE"}
+          -6: "TIMEOUT", -7: "UNSUPPORTED", -8: "STATE", -9: "CAPACITY"}
 
 
 class GridDesc(C.Structure):
@@ -79,7 +79,7 @@ EXPORTS = [
     "fsim_last_error", "fsim_stream", "fsim_synchronize", "fsim_set_particles", "fsim_add_particles",
     "fsim_get_particles", "fsim_num_particles", "fsim_set_obstacles", "fsim_get_obstacles",
     "fsim_step", "fsim_stage", "fsim_get_grid", "fsim_set_grid", "fsim_fill_gfx",
-    "fsim_set_pressure_guess", "fsim_solve_pressure",
+    "fsim_set_pressure_guess", "fsim_solve_pressure", "fsim_p2g_noalloc",
 ]
 
 _lib = None
@@ -117,6 +117,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "fsim_set_pressure_guess": (C.c_int, [P, fp, C.c_int]),
         "fsim_solve_pressure": (C.c_int, [P, dp, C.c_double, C.c_int, C.c_int, C.c_double, C.c_int, dp,
                                           C.POINTER(StepStats)]),
+        "fsim_p2g_noalloc": (C.c_int, [C.POINTER(GridDesc), C.c_int, P, P, P, i64, P, P, P, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

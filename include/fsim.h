@@ -43,6 +43,7 @@ extern "C" {
 #define FSIM_E_TIMEOUT (-6)       /* a bounded device-side wait gave up */
 #define FSIM_E_UNSUPPORTED (-7)   /* feature not built (see fsim_last_error) */
 #define FSIM_E_STATE (-8)         /* call out of order (e.g. G2P before P2G) */
+#define FSIM_E_CAPACITY (-9)      /* input larger than a fixed capacity (fsim_p2g_noalloc) */
 
 /* ---- enums ------------------------------------------------------------- */
 enum fsim_transfer { FSIM_PIC = 0, FSIM_FLIP = 1, FSIM_APIC = 2 }; /* Simulator::P2G2PType */
@@ -265,6 +266,45 @@ int fsim_set_pressure_guess(fsim_ctx *ctx, const float *p, int where);
  * the solver variants on identical inputs. */
 int fsim_solve_pressure(fsim_ctx *ctx, const double *rhs, double dt, int precision, int tol_mode,
                         double tol, int max_iters, double *p_out, fsim_step_stats *stats);
+
+/* ---- allocation-free particle-to-grid transfer --------------------------
+ * This entry point has no counterpart in the reference.  It is for callers
+ * that may not allocate GPU memory when they need a transfer: a render or
+ * game loop with a fixed frame budget (a device allocation can synchronise the
+ * device and stall the frame), a host application that owns the GPU memory
+ * pool and gives plugins only the buffers it chose, or a pipeline recorded
+ * once and replayed.  It runs the same cell sort and P2G kernels as
+ * FSIM_STAGE_P2G (Simulator::p2gTransfer + markFluidCellsAndCalculateParticleDensities)
+ * on buffers the caller owns and calls no cudaMalloc, cudaFree or other
+ * allocating routine.
+ *
+ * Scratch.  Its scratch (cell keys, ranks and the sort permutation per
+ * particle, counts and starts per cell) lives in one fixed device array of
+ * FSIM_NOALLOC_SCRATCH_BYTES compiled into the library.  Every GPU on which
+ * the library's kernels are loaded holds that array until the process exits.
+ * All calls share it and it keeps the last call's contents (the call clears the
+ * part that must start at zero), so calls whose work overlaps on the GPU --
+ * on different streams, or from different host threads -- race and must not
+ * be issued.  The first call on a device, made with that device current,
+ * looks up the array's device address (cudaGetSymbolAddress); make that first
+ * call before capturing any stream.
+ *
+ * Limits.  n <= FSIM_NOALLOC_MAX_PARTICLES and nx*ny*nz <=
+ * FSIM_NOALLOC_MAX_CELLS, else FSIM_E_CAPACITY; nz must be a multiple of 4
+ * (FSIM_E_INVALID otherwise).  Grid geometry follows fsim_grid_desc.
+ *
+ * Buffers (all device memory, stream-ordered on `stream`, a cudaStream_t or
+ * NULL for the default stream): pos and vel hold 3 planes of n floats
+ * (component a at pos + a*n), c holds 9 planes (APIC vector c[a] component b
+ * at c + (3a+b)*n; may be NULL unless transfer == FSIM_APIC).  Outputs are
+ * nx*ny*nz values in the reference cell order: face velocities vx/vy/vz,
+ * cell types in flags (WATER where a particle is, AIR elsewhere) and avgPNum. */
+#define FSIM_NOALLOC_MAX_PARTICLES (1 << 20)
+#define FSIM_NOALLOC_MAX_CELLS (1 << 20)
+#define FSIM_NOALLOC_SCRATCH_BYTES 20973312
+int fsim_p2g_noalloc(const fsim_grid_desc *grid, int transfer, const float *pos, const float *vel,
+                     const float *c, int64_t n, float *vx, float *vy, float *vz, uint8_t *flags,
+                     float *avg, void *stream);
 
 #ifdef __cplusplus
 }
