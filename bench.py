@@ -208,9 +208,10 @@ def run_fsim(args):
     grid, pos = workload_scene(res)
     h = grid.h
     dt = 1.0 / 480.0 if res == 256 else 1.0 / (480.0 * res / 256.0)
+    precond = {"mg": N.PRECOND_MG, "rbic": N.PRECOND_RBIC}[args.precond]
     p = N.default_params(transfer=N.APIC, resolution=res, tol=1e-6, tol_mode=N.TOL_REL_L2, max_iters=2000,
                          spawning=True, despawning=True, timing=True, precision=N.PREC_MIXED,
-                         warm_start=N.WARM_ZERO)
+                         warm_start=N.WARM_ZERO, precond=precond)
     sim = N.Simulation(res, p)
     sim.set_particles(pos)
     del pos
@@ -308,7 +309,7 @@ def run_fsim(args):
                    "particles": int(np_mean), "dt": dt, "pcg_tol": "1e-6 relative L2",
                    "obstacles": "moving sphere r=0.15, disc source r=4 cells, 8^3 sink box",
                    "parallelism": f"replicas x{world}", "l2": "state 8.6 GB > L2; no flush needed",
-                   "warm_start": "zero"},
+                   "warm_start": "zero", "precond": args.precond},
         "particle_steps_per_s": round(np_mean * value, 1),
         "pcg_iterations_mean": round(its, 2),
         "stage_ms": {k: round(mean(k), 3) for k in ("ms_simulate_particles", "ms_p2g", "ms_p2g_kernel", "ms_prep",
@@ -412,6 +413,8 @@ def main():
     ap.add_argument("--impl", default="fsim", choices=["fsim", "reference"])
     ap.add_argument("--res", type=int, default=256, help="grid resolution (256 = the benchmark workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precond", default="mg", choices=["mg", "rbic"],
+                    help="pressure preconditioner: multigrid V-cycle or red-black incomplete Cholesky")
     ap.add_argument("--out-dir", default=os.path.join(ROOT, "gpurun_out"))
     args = ap.parse_args()
     os.makedirs(args.out_dir, exist_ok=True)

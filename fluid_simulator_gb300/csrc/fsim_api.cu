@@ -857,8 +857,12 @@ int fsim_solve_pressure(fsim_ctx* ctx, const double* rhs, double dt, int precisi
     FSIM_CUDA_TRY(ctx, cudaMemcpyAsync(dtmp, hb.data(), (size_t)n * 8, cudaMemcpyHostToDevice, s));
     launch_dense_to_pad(g, dtmp, dpad, 8, s);
     fsim_step_stats tmp{};
-    int rc = solve_pressure(ctx, dt, precision, tol_mode, tol, max_iters, FSIM_WARM_ZERO, stats ? stats : &tmp,
-                            dpad, 0);
+    fsim_step_stats* sp = stats ? stats : &tmp;
+    cudaEventRecord(ctx->ev[EV_PREP], s);
+    int rc = solve_pressure(ctx, dt, precision, tol_mode, tol, max_iters, FSIM_WARM_ZERO, sp, dpad, 0);
+    cudaEventRecord(ctx->ev[EV_SOLVE], s);
+    cudaEventSynchronize(ctx->ev[EV_SOLVE]);
+    if (rc == FSIM_OK) sp->ms_solve = elapsed(ctx, EV_PREP, EV_SOLVE);
     if (rc == FSIM_OK && p_out) {
         launch_pad_to_dense(g, ctx->sv.phi, dtmp, 8, s);
         cudaMemcpyAsync(p_out, dtmp, (size_t)n * 8, cudaMemcpyDeviceToHost, s);

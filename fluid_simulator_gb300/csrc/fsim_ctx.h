@@ -28,6 +28,19 @@ struct PcgState {
     int nan;
     int skip;            // rhs below the reference's early-out (sum b^2 < 1e-7)
     int bufsel;          // bit 0: current r buffer, bit 1: current s buffer
+    int fold_enabled;    // MIXED: stop the inner iteration when the residual fell 100x
+    int need_fold;       // set by the iteration when a fold + restart is due
+};
+
+// One level of the multigrid hierarchy (level 0 is the simulation grid).
+struct MGLevelBufs {
+    int nx = 0, ny = 0, nz = 0, pz = 0;
+    long long ncell = 0;          // nx * ny * pz
+    uint8_t* kind = nullptr;      // 0 fluid, 1 air, 2 solid (levels >= 1)
+    uint16_t* code = nullptr;     // same encoding as SolverBufs::code
+    float* x = nullptr;           // correction (levels >= 1)
+    float* f = nullptr;           // right-hand side (levels >= 1)
+    float* r = nullptr;           // residual
 };
 
 struct SolverBufs {
@@ -51,6 +64,7 @@ struct SolverBufs {
     bool have_guess = false;
     int grid_blocks = 0;          // persistent grid size for brick kernels
     double last_scale = 1.0;      // dt / (rho h^2) of the last solve
+    std::vector<MGLevelBufs> mg;  // multigrid hierarchy (built at allocation)
 };
 
 struct fsim_ctx {

@@ -401,8 +401,11 @@ __global__ void __launch_bounds__(PCG_THREADS) k_spmv(const PcgArgs a, Vecs<T> v
     }
 }
 
-// x += alpha s; r_new = r - alpha q; black half-sweep on r_new; r.r, max|r|
-template <typename T>
+// x += alpha s; r_new = r - alpha q; r.r, max|r|; then on r_new:
+//   PMODE 1: the black half of the red-black IC solve (the red half is k_red)
+//   PMODE 2: the first red-black Gauss-Seidel sweep of the multigrid V-cycle from
+//            zero (red z = r/ns, black z = (r + sum_j r_j/ns_j)/ns)
+template <typename T, int PMODE>
 __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T> v) {
     __shared__ double scratch[32 * 2];
     if (a.st->done) return;
@@ -425,7 +428,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
         rn[c] = rv;
         rr.add(rv * rv);
         rmax = fmax(rmax, fabs(rv));
-        if ((x + y + z) & 1) {
+        if (PMODE != 0 && ((x + y + z) & 1)) {
             T sum = rv;
 #pragma unroll
             for (int k = 0; k < 6; k++)
@@ -434,7 +437,10 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
                     const uint16_t cj = a.code[j];
                     sum += (ro[j] - alpha * v.q[j]) * recip_ns<T>(code_ns(cj));
                 }
-            v.z[c] = sum * (T)black_pivot_inv(a.code, c, cc, a.B);
+            if (PMODE == 1) v.z[c] = sum * (T)black_pivot_inv(a.code, c, cc, a.B);
+            else v.z[c] = sum * recip_ns<T>(code_ns(cc));
+        } else if (PMODE == 2) {
+            v.z[c] = rv * recip_ns<T>(code_ns(cc));
         }
     }
     double acc[2] = {rr.value(), (double)rmax};
@@ -449,8 +455,334 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
             st->converged = conv ? 1 : 0;
             if (conv || st->it >= st->max_iters || !isfinite(acc[0])) st->done = 1;
             if (!isfinite(acc[0])) st->nan = 1;
+            // the FP32 recursion is trusted for a 100x residual drop, then the
+            // solution is folded into FP64 and the iteration restarts
+            if (st->fold_enabled && acc[0] < 0.01 * st->rr_update) {
+                st->need_fold = 1;
+                st->done = 1;
+            }
         }
     }
+}
+
+// z.r over all fluid cells (after a multigrid preconditioner); modes as k_red
+__global__ void __launch_bounds__(PCG_THREADS) k_dot_zr(const PcgArgs a, const float* z, const float* r0,
+                                                        const float* r1, int mode) {
+    __shared__ double scratch[32];
+    if (a.st->done) return;
+    const float* r = (a.st->bufsel & 1) ? r1 : r0;
+    Acc<float> zr;
+    const int nact = *a.nactive;
+    for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
+        int x, y, zz;
+        long long c;
+        if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, zz, c)) continue;
+        if (!(a.code[c] & CODE_FLUID)) continue;
+        zr.add(z[c] * r[c]);
+    }
+    double acc[1] = {zr.value()};
+    if (last_block_reduce<1>(acc, 0, a.partials, a.counter, scratch)) {
+        if (threadIdx.x == 0) {
+            PcgState* s = a.st;
+            const double sig = acc[0];
+            if (mode == 0) {
+                s->beta = 0.0;
+                s->sigma = sig;
+                s->sigma_prev = sig;
+            } else if (mode == 1) {
+                s->beta = sig / s->sigma;
+                s->sigma_prev = s->sigma;
+                s->sigma = sig;
+            } else {
+                s->beta = sig / s->sigma_prev;
+                s->sigma = sig;
+            }
+            if (!isfinite(s->beta)) {
+                s->nan = 1;
+                s->done = 1;
+            }
+        }
+    }
+}
+
+// ---- geometric multigrid preconditioner ------------------------------------
+//
+// z = M^-1 r by one V-cycle.  Level l + 1 halves every dimension (ceil); a
+// coarse cell is fluid if any child is fluid, else air if any child is air,
+// else solid.  Each level's operator is the same integer 7-point stencil
+// rebuilt from its own cells (rediscretisation); in the fine level's units the
+// level-l operator is L_l / 4^l, so the coarse right-hand side is
+// 4 R (f - L x) with R the full-weighting restriction (R = P^T / 8, P the
+// cell-centred trilinear prolongation, weights 3/4 and 1/4 per axis).  The
+// smoother is red-black Gauss-Seidel, NU sweeps red->black before the coarse
+// correction and black->red after it; the coarsest level (<= 512 cells) is
+// smoothed BOTTOM times each way inside one CTA.  Starting every level from
+// zero, the V-cycle is a fixed symmetric linear operator, as CG requires.
+constexpr int MG_NU_DEFAULT = 2;
+constexpr int MG_BOTTOM_SWEEPS = 32;
+constexpr int MG_BOTTOM_MAX = 4096;
+
+struct MGLev {
+    int nx, ny, nz, pz;
+    const uint16_t* code;
+    float* x;
+    const float* f;
+    const float* f1;  // level 0: the rhs is the current PCG residual buffer (r[0] or r[1])
+    float* r;
+};
+
+__device__ __forceinline__ const float* mg_rhs(const PcgArgs& A, const MGLev& L) {
+    return (L.f1 && (A.st->bufsel & 1)) ? L.f1 : L.f;
+}
+
+__device__ __forceinline__ long long mg_off(const MGLev& L, int k) {
+    const long long st = (k >> 1) == 0 ? (long long)L.pz * L.ny : ((k >> 1) == 1 ? (long long)L.pz : 1ll);
+    return (k & 1) ? -st : st;
+}
+
+// iterate over the level's cells: active bricks on level 0, all cells above
+template <bool FINE, typename F>
+__device__ __forceinline__ void mg_for_cells(const PcgArgs& A, const MGLev& L, F&& fn) {
+    if (FINE) {
+        const int nact = *A.nactive;
+        for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
+            int x, y, z;
+            long long c;
+            if (brick_cell(A.B, A.list[bk], threadIdx.x, x, y, z, c)) fn(x, y, z, c);
+        }
+    } else {
+        const long long n = (long long)L.nx * L.ny * L.nz;
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+             i += (long long)gridDim.x * blockDim.x) {
+            const int z = (int)(i % L.nz);
+            const long long t = i / L.nz;
+            const int y = (int)(t % L.ny), x = (int)(t / L.ny);
+            fn(x, y, z, ((long long)x * L.ny + y) * L.pz + z);
+        }
+    }
+}
+
+// one red-black Gauss-Seidel half sweep; first: the other colour is still zero
+template <bool FINE>
+__global__ void __launch_bounds__(PCG_THREADS) k_mg_smooth(const PcgArgs A, MGLev L, int color, int first) {
+    if (A.st->done) return;
+    const float* rhs = mg_rhs(A, L);
+    mg_for_cells<FINE>(A, L, [&](int x, int y, int z, long long c) {
+        if (((x + y + z) & 1) != color) return;
+        const uint16_t cc = L.code[c];
+        if (!(cc & CODE_FLUID)) return;
+        float sum = rhs[c];
+        if (!first) {
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                if ((cc >> k) & 1) sum += L.x[c + mg_off(L, k)];
+        }
+        L.x[c] = sum * c_rcp[code_ns(cc)];
+    });
+}
+
+// the last post-smoothing half sweep (red, level 0) fused with z.r (modes as k_red)
+__global__ void __launch_bounds__(PCG_THREADS) k_mg_smooth_dot(const PcgArgs A, MGLev L, int mode) {
+    __shared__ double scratch[32];
+    if (A.st->done) return;
+    const float* rhs = mg_rhs(A, L);
+    Acc<float> zr;
+    mg_for_cells<true>(A, L, [&](int x, int y, int z, long long c) {
+        const uint16_t cc = L.code[c];
+        if (!(cc & CODE_FLUID)) return;
+        const float rv = rhs[c];
+        float zv;
+        if (((x + y + z) & 1) == 0) {
+            float sum = rv;
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                if ((cc >> k) & 1) sum += L.x[c + mg_off(L, k)];
+            zv = sum * c_rcp[code_ns(cc)];
+            L.x[c] = zv;
+        } else {
+            zv = L.x[c];
+        }
+        zr.add(zv * rv);
+    });
+    double acc[1] = {zr.value()};
+    if (last_block_reduce<1>(acc, 0, A.partials, A.counter, scratch)) {
+        if (threadIdx.x == 0) {
+            PcgState* s = A.st;
+            const double sig = acc[0];
+            if (mode == 0) {
+                s->beta = 0.0;
+                s->sigma = sig;
+                s->sigma_prev = sig;
+            } else {
+                s->beta = sig / s->sigma;
+                s->sigma_prev = s->sigma;
+                s->sigma = sig;
+            }
+            if (!isfinite(s->beta)) {
+                s->nan = 1;
+                s->done = 1;
+            }
+        }
+    }
+}
+
+template <bool FINE>
+__global__ void __launch_bounds__(PCG_THREADS) k_mg_residual(const PcgArgs A, MGLev L) {
+    if (A.st->done) return;
+    const float* rhs = mg_rhs(A, L);
+    mg_for_cells<FINE>(A, L, [&](int x, int y, int z, long long c) {
+        const uint16_t cc = L.code[c];
+        if (!(cc & CODE_FLUID)) return;
+        float ax = (float)code_ns(cc) * L.x[c];
+#pragma unroll
+        for (int k = 0; k < 6; k++)
+            if ((cc >> k) & 1) ax -= L.x[c + mg_off(L, k)];
+        L.r[c] = rhs[c] - ax;
+    });
+}
+
+// coarse f = 0.5 * sum_fine P[f,C] r_f  (= 4 R r); coarse cells, dense
+__global__ void __launch_bounds__(PCG_THREADS) k_mg_restrict(const PcgState* st, MGLev F, MGLev Cl) {
+    if (st->done) return;
+    const long long n = (long long)Cl.nx * Cl.ny * Cl.nz;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int cz = (int)(i % Cl.nz);
+        const long long t = i / Cl.nz;
+        const int cy = (int)(t % Cl.ny), cx = (int)(t / Cl.ny);
+        const long long cidx = ((long long)cx * Cl.ny + cy) * Cl.pz + cz;
+        if (!(Cl.code[cidx] & CODE_FLUID)) continue;
+        float sum = 0.f;
+        for (int dx = -1; dx <= 2; dx++) {
+            const int fx = 2 * cx + dx;
+            if (fx < 0 || fx >= F.nx) continue;
+            const float wx = (dx == 0 || dx == 1) ? 0.75f : 0.25f;
+            for (int dy = -1; dy <= 2; dy++) {
+                const int fy = 2 * cy + dy;
+                if (fy < 0 || fy >= F.ny) continue;
+                const float wxy = wx * ((dy == 0 || dy == 1) ? 0.75f : 0.25f);
+                const long long row = ((long long)fx * F.ny + fy) * F.pz;
+#pragma unroll
+                for (int dz = -1; dz <= 2; dz++) {
+                    const int fz = 2 * cz + dz;
+                    if (fz < 0 || fz >= F.nz) continue;
+                    if (!(F.code[row + fz] & CODE_FLUID)) continue;
+                    sum += wxy * ((dz == 0 || dz == 1) ? 0.75f : 0.25f) * F.r[row + fz];
+                }
+            }
+        }
+        const_cast<float*>(Cl.f)[cidx] = 0.5f * sum;
+    }
+}
+
+// fine x += P x_coarse on fluid fine cells
+template <bool FINE>
+__global__ void __launch_bounds__(PCG_THREADS) k_mg_prolong(const PcgArgs A, MGLev F, MGLev Cl) {
+    if (A.st->done) return;
+    mg_for_cells<FINE>(A, F, [&](int x, int y, int z, long long c) {
+        if (!(F.code[c] & CODE_FLUID)) return;
+        const int px = (x & 1) ? x >> 1 : (x >> 1) - 1;  // lower coarse neighbour per axis
+        const int py = (y & 1) ? y >> 1 : (y >> 1) - 1;
+        const int pz = (z & 1) ? z >> 1 : (z >> 1) - 1;
+        const float wlx = (x & 1) ? 0.75f : 0.25f, wly = (y & 1) ? 0.75f : 0.25f, wlz = (z & 1) ? 0.75f : 0.25f;
+        float sum = 0.f;
+#pragma unroll
+        for (int o = 0; o < 8; o++) {
+            const int ox = o >> 2, oy = (o >> 1) & 1, oz = o & 1;
+            const int cx = px + ox, cy = py + oy, cz = pz + oz;
+            if (cx < 0 || cy < 0 || cz < 0 || cx >= Cl.nx || cy >= Cl.ny || cz >= Cl.nz) continue;
+            const long long ci = ((long long)cx * Cl.ny + cy) * Cl.pz + cz;
+            if (!(Cl.code[ci] & CODE_FLUID)) continue;
+            const float w = (ox ? 1.f - wlx : wlx) * (oy ? 1.f - wly : wly) * (oz ? 1.f - wlz : wlz);
+            sum += w * Cl.x[ci];
+        }
+        F.x[c] += sum;
+    });
+}
+
+// coarsest level: symmetric red-black Gauss-Seidel in shared memory, one CTA
+__global__ void __launch_bounds__(1024) k_mg_bottom(const PcgState* st, MGLev L) {
+    if (st->done) return;
+    __shared__ float sx[MG_BOTTOM_MAX];
+    __shared__ float sf[MG_BOTTOM_MAX];
+    __shared__ uint16_t sc[MG_BOTTOM_MAX];
+    const int n = L.nx * L.ny * L.nz;  // dense (pz == nz)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        sx[i] = 0.f;
+        sf[i] = L.f[i];
+        sc[i] = L.code[i];
+    }
+    __syncthreads();
+    const int sxs = L.ny * L.nz, sys = L.nz;
+    for (int pass = 0; pass < 2 * MG_BOTTOM_SWEEPS; pass++) {
+        // forward half: red then black; backward half: black then red
+        for (int h = 0; h < 2; h++) {
+            const int color = (pass < MG_BOTTOM_SWEEPS) ? h : 1 - h;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const int z = i % L.nz, y = (i / L.nz) % L.ny, x = i / sxs;
+                if (((x + y + z) & 1) != color) continue;
+                const uint16_t cc = sc[i];
+                if (!(cc & CODE_FLUID)) continue;
+                float sum = sf[i];
+                if (cc & 1) sum += sx[i + sxs];
+                if (cc & 2) sum += sx[i - sxs];
+                if (cc & 4) sum += sx[i + sys];
+                if (cc & 8) sum += sx[i - sys];
+                if (cc & 16) sum += sx[i + 1];
+                if (cc & 32) sum += sx[i - 1];
+                sx[i] = sum * c_rcp[code_ns(cc)];
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) L.x[i] = sx[i];
+}
+
+// coarse cell kinds: fluid if any child is fluid, else air if any child is air
+__global__ void k_mg_coarsen(MGLev F, const uint8_t* fkind, const uint8_t* fflags, MGLev Cl, uint8_t* ckind) {
+    const long long n = (long long)Cl.nx * Cl.ny * Cl.nz;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int cz = (int)(i % Cl.nz);
+    const long long t = i / Cl.nz;
+    const int cy = (int)(t % Cl.ny), cx = (int)(t / Cl.ny);
+    int best = 2;
+    for (int o = 0; o < 8; o++) {
+        const int fx = 2 * cx + (o >> 2), fy = 2 * cy + ((o >> 1) & 1), fz = 2 * cz + (o & 1);
+        if (fx >= F.nx || fy >= F.ny || fz >= F.nz) continue;
+        const long long fi = ((long long)fx * F.ny + fy) * F.pz + fz;
+        int k;
+        if (fkind) k = fkind[fi];
+        else k = (F.code[fi] & CODE_FLUID) ? 0 : (fflags[fi] == C_AIR ? 1 : 2);
+        best = min(best, k);
+    }
+    ckind[i] = (uint8_t)best;
+}
+
+// per-cell code of a coarse level from its kinds (outside the level = solid)
+__global__ void k_mg_code(MGLev L, const uint8_t* kind, uint16_t* code) {
+    const long long n = (long long)L.nx * L.ny * L.nz;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int z = (int)(i % L.nz);
+    const long long t = i / L.nz;
+    const int y = (int)(t % L.ny), x = (int)(t / L.ny);
+    if (kind[i] != 0) {
+        code[i] = 0;
+        return;
+    }
+    uint16_t cd = CODE_FLUID;
+    int ns = 0;
+    const int pos[3] = {x, y, z}, lim[3] = {L.nx, L.ny, L.nz};
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const int a = k >> 1, dir = (k & 1) ? -1 : 1;
+        const int q = pos[a] + dir;
+        if (q < 0 || q >= lim[a]) continue;
+        const uint8_t kn = kind[i + mg_off(L, k)];
+        if (kn == 0) cd |= (uint16_t)(1u << k);
+        if (kn != 2) ns++;
+    }
+    code[i] = cd | (uint16_t)(ns << 8);
 }
 
 // phi += x; x = 0   (fold the FP32 accumulator into the FP64 solution)
@@ -495,7 +827,7 @@ int solver_alloc(fsim_ctx* ctx) {
     S.q = S.r + 5 * nc;
     S.plo = S.r + 6 * nc;
     int bps = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_update<float>, PCG_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_update<float, 1>, PCG_THREADS, 0);
     if (bps < 1) bps = 1;
     S.grid_blocks = ctx->num_sms * bps;
     FSIM_CUDA_TRY(ctx, cudaMalloc(&S.partials, (size_t)S.grid_blocks * 4 * sizeof(double)));
@@ -511,7 +843,105 @@ int solver_alloc(fsim_ctx* ctx) {
     float rcp[7];
     for (int ns = 0; ns < 7; ns++) rcp[ns] = ns > 0 ? 1.f / ns : 1.f;
     FSIM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rcp, rcp, sizeof(rcp)));
+    // multigrid hierarchy: halve until every dimension is <= 8
+    MGLevelBufs l0;
+    l0.nx = g.nx; l0.ny = g.ny; l0.nz = g.nz; l0.pz = g.pz; l0.ncell = g.ncell;
+    l0.code = S.code;
+    FSIM_CUDA_TRY(ctx, cudaMalloc(&l0.r, nc * sizeof(float)));
+    S.mg.push_back(l0);
+    while (std::max(S.mg.back().nx, std::max(S.mg.back().ny, S.mg.back().nz)) > 8) {
+        const MGLevelBufs& f = S.mg.back();
+        MGLevelBufs c;
+        c.nx = (f.nx + 1) / 2; c.ny = (f.ny + 1) / 2; c.nz = (f.nz + 1) / 2; c.pz = c.nz;
+        c.ncell = (long long)c.nx * c.ny * c.nz;
+        FSIM_CUDA_TRY(ctx, cudaMalloc(&c.kind, c.ncell));
+        FSIM_CUDA_TRY(ctx, cudaMalloc(&c.code, c.ncell * sizeof(uint16_t)));
+        FSIM_CUDA_TRY(ctx, cudaMalloc(&c.x, c.ncell * sizeof(float)));
+        FSIM_CUDA_TRY(ctx, cudaMalloc(&c.f, c.ncell * sizeof(float)));
+        FSIM_CUDA_TRY(ctx, cudaMalloc(&c.r, c.ncell * sizeof(float)));
+        FSIM_CUDA_TRY(ctx, cudaMemset(c.x, 0, c.ncell * sizeof(float)));
+        S.mg.push_back(c);
+    }
+    if (S.mg.back().ncell > MG_BOTTOM_MAX) {
+        ctx->err = "multigrid coarsest level too large";
+        return FSIM_E_INVALID;
+    }
     return FSIM_OK;
+}
+
+static MGLev mg_lev(const SolverBufs& S, int l, const float* f0, const float* f1, float* x0) {
+    const MGLevelBufs& b = S.mg[l];
+    MGLev L;
+    L.nx = b.nx; L.ny = b.ny; L.nz = b.nz; L.pz = b.pz;
+    L.code = b.code;
+    L.r = b.r;
+    if (l == 0) {
+        L.x = x0; L.f = f0; L.f1 = f1;
+    } else {
+        L.x = b.x; L.f = b.f; L.f1 = nullptr;
+    }
+    return L;
+}
+
+// per-solve: coarse cell kinds and codes from the fine flags
+static void mg_setup(fsim_ctx* ctx) {
+    SolverBufs& S = ctx->sv;
+    cudaStream_t st = ctx->stream;
+    for (size_t l = 1; l < S.mg.size(); l++) {
+        MGLev F = mg_lev(S, (int)l - 1, nullptr, nullptr, nullptr);
+        MGLev Cl = mg_lev(S, (int)l, nullptr, nullptr, nullptr);
+        const long long n = S.mg[l].ncell;
+        k_mg_coarsen<<<ceil_div(n, 256), 256, 0, st>>>(F, l == 1 ? nullptr : S.mg[l - 1].kind, ctx->flags, Cl,
+                                                       S.mg[l].kind);
+        k_mg_code<<<ceil_div(n, 256), 256, 0, st>>>(Cl, S.mg[l].kind, S.mg[l].code);
+        ctx->launches += 2;
+    }
+}
+
+// z = V-cycle(r); r is the current PCG residual (r0 or r1 by device state).
+// first_fused: the first level-0 sweep was done by k_update; dot_mode >= 0: the
+// last level-0 sweep also computes z.r and the CG scalars (k_red modes).
+static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, const float* r1, float* z,
+                      bool first_fused, int dot_mode) {
+    const int NU = ctx->prm.mg_sweeps > 0 ? ctx->prm.mg_sweeps : MG_NU_DEFAULT;
+    SolverBufs& S = ctx->sv;
+    cudaStream_t st = ctx->stream;
+    const int G = S.grid_blocks;
+    MGLev L = mg_lev(S, l, r0, r1, z);
+    const int last = (int)S.mg.size() - 1;
+    if (l == last) {
+        k_mg_bottom<<<1, 1024, 0, st>>>(A.st, L);
+        ctx->launches += 1;
+        return;
+    }
+    const int nb = l == 0 ? G : std::min(G, ceil_div(S.mg[l].ncell, 256));
+    auto smooth = [&](int color, int first) {
+        if (l == 0) k_mg_smooth<true><<<nb, PCG_THREADS, 0, st>>>(A, L, color, first);
+        else k_mg_smooth<false><<<nb, PCG_THREADS, 0, st>>>(A, L, color, first);
+    };
+    for (int k = 0; k < NU; k++) {
+        if (k == 0 && l == 0 && first_fused) continue;
+        smooth(0, k == 0);
+        smooth(1, 0);
+        ctx->launches += 2;
+    }
+    if (l == 0) k_mg_residual<true><<<nb, PCG_THREADS, 0, st>>>(A, L);
+    else k_mg_residual<false><<<nb, PCG_THREADS, 0, st>>>(A, L);
+    MGLev Cl = mg_lev(S, l + 1, nullptr, nullptr, nullptr);
+    const int nbc = std::min(G, ceil_div(S.mg[l + 1].ncell, 256));
+    k_mg_restrict<<<nbc, PCG_THREADS, 0, st>>>(A.st, L, Cl);
+    mg_vcycle(ctx, A, l + 1, nullptr, nullptr, nullptr, false, -1);
+    if (l == 0) k_mg_prolong<true><<<nb, PCG_THREADS, 0, st>>>(A, L, Cl);
+    else k_mg_prolong<false><<<nb, PCG_THREADS, 0, st>>>(A, L, Cl);
+    for (int k = 0; k < NU; k++) {
+        smooth(1, 0);
+        if (l == 0 && k == NU - 1 && dot_mode >= 0)
+            k_mg_smooth_dot<<<nb, PCG_THREADS, 0, st>>>(A, L, dot_mode);
+        else
+            smooth(0, 0);
+        ctx->launches += 2;
+    }
+    ctx->launches += 3;
 }
 
 static int alloc_fp64(fsim_ctx* ctx) {
@@ -531,60 +961,83 @@ void solver_free(fsim_ctx* ctx) {
     cudaFree(S.brick_list); cudaFree(S.d_nactive); cudaFree(S.brick_flag); cudaFree(S.code);
     cudaFree(S.b); cudaFree(S.phi); cudaFree(S.r); cudaFree(S.r64); cudaFree(S.partials);
     cudaFree(S.counter); cudaFree(S.st); cudaFreeHost(S.st_host); cudaFree(S.guess);
+    for (size_t l = 0; l < S.mg.size(); l++) {
+        cudaFree(S.mg[l].r);
+        if (l > 0) {
+            cudaFree(S.mg[l].kind); cudaFree(S.mg[l].code); cudaFree(S.mg[l].x); cudaFree(S.mg[l].f);
+        }
+    }
     S = SolverBufs{};
 }
 
 template <typename T>
-static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, fsim_step_stats* stats) {
+static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, int precond, fsim_step_stats* stats) {
     SolverBufs& S = ctx->sv;
     cudaStream_t st = ctx->stream;
     const int G = S.grid_blocks;
     const bool fold = (precision == FSIM_PREC_MIXED);
+    const bool mg = (precond == FSIM_PRECOND_MG) && sizeof(T) == 4;
     int folds = 0;
     auto read_state = [&]() -> int {
         FSIM_CUDA_TRY(ctx, cudaMemcpyAsync(S.st_host, S.st, sizeof(PcgState), cudaMemcpyDeviceToHost, st));
         FSIM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
         return FSIM_OK;
     };
+    // z = M^-1 r and sigma (mode 0 setup, 1 iteration, 2 after a fold)
+    auto precondition = [&](int mode, bool black_done) {
+        if (mg) {
+            // mode 1: k_update already did the first sweep; the V-cycle ends with z.r
+            mg_vcycle(ctx, A, 0, (const float*)(const void*)v.r[0], (const float*)(const void*)v.r[1],
+                      (float*)(void*)v.z, mode == 1, mode);
+        } else {
+            if (!black_done) {
+                k_black<T><<<G, PCG_THREADS, 0, st>>>(A, v);
+                ctx->launches += 1;
+            }
+            k_red<T><<<G, PCG_THREADS, 0, st>>>(A, v, mode);
+            ctx->launches += 1;
+        }
+    };
+    if (mg) mg_setup(ctx);
     // initial residual, preconditioned residual, sigma
     k_residual<T><<<G, PCG_THREADS, 0, st>>>(A, v, 1, 1);
-    k_black<T><<<G, PCG_THREADS, 0, st>>>(A, v);
-    k_red<T><<<G, PCG_THREADS, 0, st>>>(A, v, 0);
-    ctx->launches += 3;
+    ctx->launches += 1;
+    precondition(0, false);
     fsim_record(ctx, EV_PCG_SETUP);
     int rc = read_state();
     if (rc) return rc;
-    int chunk = 4;
+    int chunk = mg ? 2 : 4;
+    const int chunk_max = mg ? 8 : 16;
     while (!S.st_host->done && !S.st_host->nan) {
         for (int k = 0; k < chunk; k++) {
             k_spmv<T><<<G, PCG_THREADS, 0, st>>>(A, v);
-            k_update<T><<<G, PCG_THREADS, 0, st>>>(A, v);
-            k_red<T><<<G, PCG_THREADS, 0, st>>>(A, v, 1);
+            if (mg) k_update<T, 2><<<G, PCG_THREADS, 0, st>>>(A, v);
+            else k_update<T, 1><<<G, PCG_THREADS, 0, st>>>(A, v);
+            ctx->launches += 2;
+            precondition(1, true);
         }
-        ctx->launches += 3 * chunk;
         if ((rc = read_state())) return rc;
-        if (chunk < 16) chunk *= 2;
+        if (chunk < chunk_max) chunk *= 2;
         PcgState& h = *S.st_host;
         if (h.nan) break;
-        const bool need_fold = fold && (h.done || h.rr < 0.01 * h.rr_update);
+        const bool need_fold = fold && (h.need_fold || h.done);
         if (need_fold && !h.skip) {
-            // fold, recompute the true residual in FP64, restart the preconditioned residual
+            // fold the FP32 correction into the FP64 solution, recompute the true
+            // residual in FP64, and restart CG from it (s = M^-1 r, beta = 0)
             k_fold<<<G, PCG_THREADS, 0, st>>>(A, (float*)(void*)v.x);
             const int it_before = h.it;
-            const int was_done = h.done;
             h.done = 0;
+            h.need_fold = 0;
             FSIM_CUDA_TRY(ctx, cudaMemcpyAsync(&S.st->done, &h.done, sizeof(int), cudaMemcpyHostToDevice, st));
+            FSIM_CUDA_TRY(ctx, cudaMemcpyAsync(&S.st->need_fold, &h.need_fold, sizeof(int), cudaMemcpyHostToDevice, st));
             k_residual<T><<<G, PCG_THREADS, 0, st>>>(A, v, 0, 0);
-            k_black<T><<<G, PCG_THREADS, 0, st>>>(A, v);
-            k_red<T><<<G, PCG_THREADS, 0, st>>>(A, v, 2);
-            ctx->launches += 4;
+            ctx->launches += 2;
+            precondition(0, false);
             folds++;
             if ((rc = read_state())) return rc;
-            if (!h.done && it_before >= h.max_iters) {
-                h.done = 1;
-            }
-            (void)was_done;
+            if (!h.done && it_before >= h.max_iters) h.done = 1;
             if (h.done) break;
+            chunk = mg ? 2 : 4;
         } else if (h.done) {
             break;
         }
@@ -649,6 +1102,7 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     h.tol_mode = tol_mode;
     h.max_iters = max_iters;
     h.tol_abs = tol / scale;
+    h.fold_enabled = (precision == FSIM_PREC_MIXED) ? 1 : 0;
     *S.st_host = h;
     FSIM_CUDA_TRY(ctx, cudaMemcpyAsync(S.st, S.st_host, sizeof(PcgState), cudaMemcpyHostToDevice, st));
 
@@ -675,7 +1129,7 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
         v.s[0] = S.s64; v.s[1] = S.s64 + nc;
         v.z = S.z64; v.q = S.q64;
         v.x = S.phi;
-        rc = run_pcg<double>(ctx, A, v, precision, stats);
+        rc = run_pcg<double>(ctx, A, v, precision, FSIM_PRECOND_RBIC, stats);
     } else {
         const size_t nc = (size_t)g.ncell;
         Vecs<float> v;
@@ -683,7 +1137,7 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
         v.s[0] = S.s; v.s[1] = S.s + nc;
         v.z = S.z; v.q = S.q;
         v.x = S.plo;
-        rc = run_pcg<float>(ctx, A, v, precision, stats);
+        rc = run_pcg<float>(ctx, A, v, precision, ctx->prm.precond, stats);
     }
     if (rc) return rc;
     PcgState& hs = *S.st_host;

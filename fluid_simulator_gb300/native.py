@@ -23,6 +23,7 @@ OBS_SPHERE, OBS_BOX, OBS_SOURCE, OBS_SINK, OBS_DISC_SOURCE, OBS_BOX_SINK = range
 TOL_ABS_MAX, TOL_REL_L2 = 0, 1
 PREC_MIXED, PREC_FP32, PREC_FP64 = 0, 1, 2
 WARM_ZERO, WARM_PREVIOUS, WARM_GUESS = 0, 1, 2
+PRECOND_RBIC, PRECOND_MG = 0, 1
 (STAGE_SPAWN, STAGE_ADVECT, STAGE_PUSH_APART, STAGE_PUSH_OUT, STAGE_STOP, STAGE_P2G, STAGE_MARK,
  STAGE_OBSTACLES, STAGE_WALLS, STAGE_POST_P2G, STAGE_SOLVE, STAGE_EXTRAPOLATE, STAGE_G2P) = range(13)
 (F_FLAGS, F_AVGPNUM, F_VX, F_VY, F_VZ, F_V2X, F_V2Y, F_V2Z, F_PRESSURE, F_COUNT,
@@ -44,7 +45,8 @@ class Params(C.Structure):
         ("pressure_enabled", C.c_int), ("pressure_k", C.c_double), ("average_pressure", C.c_double),
         ("max_iters", C.c_int), ("fluid_density", C.c_double), ("residual_tol", C.c_double),
         ("tol_mode", C.c_int), ("particle_r", C.c_double), ("precision", C.c_int),
-        ("warm_start", C.c_int), ("track_ids", C.c_int), ("timing", C.c_int), ("reserved", C.c_int * 7),
+        ("warm_start", C.c_int), ("track_ids", C.c_int), ("timing", C.c_int), ("precond", C.c_int),
+        ("mg_sweeps", C.c_int), ("reserved", C.c_int * 5),
     ]
 
 
@@ -137,7 +139,8 @@ def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: 
                    top_solid: bool = True, particle_r: float | None = None, spawning: bool = False,
                    despawning: bool = False, stop_particles: bool = False, gravity_enabled: bool = True,
                    pressure_enabled: bool = False, pressure_k: float = 2.0, average_pressure: float = 2.0,
-                   fluid_density: float = 1.0, timing: bool = False) -> Params:
+                   fluid_density: float = 1.0, timing: bool = False, precond: int = PRECOND_MG,
+                   mg_sweeps: int = 0) -> Params:
     """Parameters of the dam-break workloads (reference parameter names in fsim.h)."""
     p = Params()
     p.transfer = transfer
@@ -162,6 +165,8 @@ def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: 
     p.warm_start = warm_start
     p.track_ids = 0
     p.timing = int(timing)
+    p.precond = precond
+    p.mg_sweeps = mg_sweeps
     return p
 
 

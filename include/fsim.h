@@ -74,6 +74,12 @@ enum fsim_precision {
     FSIM_PREC_FP64 = 2   /* all-FP64 PCG (precision-study oracle on the device) */
 };
 
+/* Preconditioner of the pressure solve. */
+enum fsim_precond {
+    FSIM_PRECOND_RBIC = 0, /* incomplete Cholesky in red-black order (modified, tau 0.97) */
+    FSIM_PRECOND_MG = 1    /* geometric multigrid V-cycle (red-black Gauss-Seidel smoothing) */
+};
+
 /* Initial guess of the pressure solve. */
 enum fsim_warm_start {
     FSIM_WARM_ZERO = 0,     /* p0 = 0, as the reference */
@@ -144,7 +150,9 @@ typedef struct fsim_params {
     int warm_start;         /* fsim_warm_start */
     int track_ids;          /* keep a stable id per particle (fsim_get_particles in id order) */
     int timing;             /* record per-stage CUDA-event times into fsim_step_stats */
-    int reserved[7];
+    int precond;            /* fsim_precond (FSIM_PREC_FP64 always uses FSIM_PRECOND_RBIC) */
+    int mg_sweeps;          /* multigrid smoothing sweeps before and after the coarse correction (0: 2) */
+    int reserved[5];
 } fsim_params;
 
 /* Obstacle (obstacles.hpp:7-65), speed set by the caller as (pos-prevPos)/dt. */

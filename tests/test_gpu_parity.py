@@ -69,12 +69,13 @@ def test_first_step_stages_chained(gpu, port_lib):
         assert_close_field(g.grid(fg), o.grid(fo), REL_GRID, f"field {fg}")
 
 
-@pytest.mark.parametrize("precision", [N.PREC_MIXED, N.PREC_FP64])
-def test_pressure_matches_oracle(gpu, port_lib, precision):
+@pytest.mark.parametrize("precision,precond", [(N.PREC_MIXED, N.PRECOND_MG), (N.PREC_MIXED, N.PRECOND_RBIC),
+                                              (N.PREC_FP64, N.PRECOND_RBIC)])
+def test_pressure_matches_oracle(gpu, port_lib, precision, precond):
     """Same flags and v2 on both sides; both solve to a tight tolerance."""
     pos, vel, c = moving_state(32, N.FLIP)
     g, o = make_pair(pos, 32, N.FLIP, vel=vel, threads=4, tol=1e-11, max_iters=2000,
-                     gpu_tol=1e-11, gpu_tol_mode=N.TOL_ABS_MAX, precision=precision)
+                     gpu_tol=1e-11, gpu_tol_mode=N.TOL_ABS_MAX, precision=precision, precond=precond)
     g.stage(N.STAGE_P2G, DT32)
     for st in (O.STAGE_P2G, O.STAGE_MARK, O.STAGE_OBSTACLES, O.STAGE_WALLS, O.STAGE_POST_P2G):
         o.stage(st, DT32)
@@ -88,6 +89,23 @@ def test_pressure_matches_oracle(gpu, port_lib, precision):
     assert_close_field(g.grid(N.F_PRESSURE), o.grid(O.F_PRESSURE), REL_PRESSURE, "pressure")
     for fg, fo in ((N.F_V2X, O.F_V2X), (N.F_V2Y, O.F_V2Y), (N.F_V2Z, O.F_V2Z)):
         assert_close_field(g.grid(fg), o.grid(fo), REL_GRID * 10, f"v2 after projection {fg}")
+
+
+def test_multigrid_needs_far_fewer_iterations(gpu, port_lib):
+    """Both preconditioners reach the same pressure; multigrid in far fewer iterations."""
+    pos, vel, c = moving_state(32, N.FLIP)
+    result = {}
+    for precond in (N.PRECOND_RBIC, N.PRECOND_MG):
+        g, o = make_pair(pos, 32, N.FLIP, vel=vel, gpu_tol=1e-8, gpu_tol_mode=N.TOL_REL_L2, gpu_max_iters=3000,
+                         precond=precond)
+        g.stage(N.STAGE_P2G, DT32)
+        for st in (N.STAGE_OBSTACLES, N.STAGE_WALLS, N.STAGE_POST_P2G):
+            g.stage(st, DT32)
+        stats = g.stage(N.STAGE_SOLVE, DT32)
+        assert stats.converged == 1
+        result[precond] = (stats.pcg_iterations, g.grid(N.F_PRESSURE))
+    assert result[N.PRECOND_MG][0] * 3 < result[N.PRECOND_RBIC][0]
+    assert_close_field(result[N.PRECOND_MG][1], result[N.PRECOND_RBIC][1], 1e-5, "pressure MG vs RB-IC")
 
 
 def test_extrapolation_matches_oracle(gpu, port_lib):
