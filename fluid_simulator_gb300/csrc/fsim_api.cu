@@ -808,12 +808,31 @@ int fsim_fill_gfx(fsim_ctx* ctx, fsim_particle_gfx* out, int64_t cap, int64_t* n
     fsim_particle_gfx* dst = out;
     void* tmp = nullptr;
     if (where == FSIM_HOST) {
-        FSIM_CUDA_TRY(ctx, cudaMallocAsync(&tmp, (size_t)n * sizeof(fsim_particle_gfx), s));
-        dst = (fsim_particle_gfx*)tmp;
+        // Write straight into host memory when the GPU can address it: pinned or
+        // registered buffers through their device alias, any host buffer on
+        // systems with coherent access to pageable memory (NVLink-C2C hosts).
+        cudaPointerAttributes attr{};
+        void* alias = nullptr;
+        int pageable = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, ctx->device);
+        if (cudaPointerGetAttributes(&attr, out) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+            attr.devicePointer != nullptr) {
+            alias = attr.devicePointer;
+        } else if (pageable) {
+            alias = out;
+        }
+        cudaGetLastError();
+        if (alias) {
+            dst = (fsim_particle_gfx*)alias;
+        } else {
+            FSIM_CUDA_TRY(ctx, cudaMallocAsync(&tmp, (size_t)n * sizeof(fsim_particle_gfx), s));
+            dst = (fsim_particle_gfx*)tmp;
+        }
     }
     launch_gfx(ctx->buf[ctx->cur], n, ctx->avg, ctx->g, dst, s);
+    ctx->launches += 1;
     CHECK_LAUNCH(ctx);
-    if (where == FSIM_HOST) {
+    if (tmp) {
         FSIM_CUDA_TRY(ctx, cudaMemcpyAsync(out, tmp, (size_t)n * sizeof(fsim_particle_gfx), cudaMemcpyDeviceToHost, s));
         FSIM_CUDA_TRY(ctx, cudaFreeAsync(tmp, s));
     }

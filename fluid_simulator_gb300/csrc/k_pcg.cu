@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_residual(const PcgArgs a, Vecs<
                 s->tol_rel2 = a.tol_rel * a.tol_rel * acc[2];
                 s->skip = acc[2] < a.skip_bb ? 1 : 0;
             }
-            const bool conv = (s->tol_mode == FSIM_TOL_ABS_MAX) ? (acc[1] < a.tol_abs) : (acc[0] <= s->tol_rel2);
+            const bool conv = (s->tol_mode == FSIM_TOL_ABS_MAX) ? (acc[1] < s->tol_abs) : (acc[0] <= s->tol_rel2);
             s->converged = conv ? 1 : 0;
             s->done = (conv || s->skip) ? 1 : 0;
         }
@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
             st->rmax = acc[1];
             st->it += 1;
             st->bufsel ^= 1;  // r buffers swap
-            const bool conv = (st->tol_mode == FSIM_TOL_ABS_MAX) ? (acc[1] < a.tol_abs) : (acc[0] <= st->tol_rel2);
+            const bool conv = (st->tol_mode == FSIM_TOL_ABS_MAX) ? (acc[1] < st->tol_abs) : (acc[0] <= st->tol_rel2);
             st->converged = conv ? 1 : 0;
             if (conv || st->it >= st->max_iters || !isfinite(acc[0])) st->done = 1;
             if (!isfinite(acc[0])) st->nan = 1;
@@ -460,46 +460,6 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
             if (st->fold_enabled && acc[0] < 0.01 * st->rr_update) {
                 st->need_fold = 1;
                 st->done = 1;
-            }
-        }
-    }
-}
-
-// z.r over all fluid cells (after a multigrid preconditioner); modes as k_red
-__global__ void __launch_bounds__(PCG_THREADS) k_dot_zr(const PcgArgs a, const float* z, const float* r0,
-                                                        const float* r1, int mode) {
-    __shared__ double scratch[32];
-    if (a.st->done) return;
-    const float* r = (a.st->bufsel & 1) ? r1 : r0;
-    Acc<float> zr;
-    const int nact = *a.nactive;
-    for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
-        int x, y, zz;
-        long long c;
-        if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, zz, c)) continue;
-        if (!(a.code[c] & CODE_FLUID)) continue;
-        zr.add(z[c] * r[c]);
-    }
-    double acc[1] = {zr.value()};
-    if (last_block_reduce<1>(acc, 0, a.partials, a.counter, scratch)) {
-        if (threadIdx.x == 0) {
-            PcgState* s = a.st;
-            const double sig = acc[0];
-            if (mode == 0) {
-                s->beta = 0.0;
-                s->sigma = sig;
-                s->sigma_prev = sig;
-            } else if (mode == 1) {
-                s->beta = sig / s->sigma;
-                s->sigma_prev = s->sigma;
-                s->sigma = sig;
-            } else {
-                s->beta = sig / s->sigma_prev;
-                s->sigma = sig;
-            }
-            if (!isfinite(s->beta)) {
-                s->nan = 1;
-                s->done = 1;
             }
         }
     }
@@ -519,7 +479,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_dot_zr(const PcgArgs a, const f
 // smoothed BOTTOM times each way inside one CTA.  Starting every level from
 // zero, the V-cycle is a fixed symmetric linear operator, as CG requires.
 constexpr int MG_NU_DEFAULT = 2;
-constexpr int MG_BOTTOM_SWEEPS = 32;
+constexpr int MG_BOTTOM_SWEEPS = 12;
 constexpr int MG_BOTTOM_MAX = 4096;
 
 struct MGLev {
@@ -540,69 +500,142 @@ __device__ __forceinline__ long long mg_off(const MGLev& L, int k) {
     return (k & 1) ? -st : st;
 }
 
-// iterate over the level's cells: active bricks on level 0, all cells above
+// ---- quad kernels -----------------------------------------------------------
+// Every multigrid kernel (and the MG-path PCG kernels) gives each thread a quad:
+// four consecutive z cells of one row, 16-byte aligned (every level pads z to
+// a multiple of 4).  The centre and the +-x / +-y neighbour quads are single
+// float4 loads, the +-z neighbours come from the quad itself plus one scalar on
+// either side, and the four cell codes are one 8-byte load.  Level 0 walks the
+// active bricks (64 quads per 2x4x32 brick, four bricks per 256-thread pass);
+// coarser levels walk all their quads.
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, const float (&v)[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void unpack4(const float4 f, float (&v)[4]) {
+    v[0] = f.x; v[1] = f.y; v[2] = f.z; v[3] = f.w;
+}
+__device__ __forceinline__ void codes4(const uint16_t* code, long long c0, uint16_t (&cc)[4]) {
+    const uint2 w = *reinterpret_cast<const uint2*>(code + c0);
+    cc[0] = (uint16_t)(w.x & 0xFFFFu);
+    cc[1] = (uint16_t)(w.x >> 16);
+    cc[2] = (uint16_t)(w.y & 0xFFFFu);
+    cc[3] = (uint16_t)(w.y >> 16);
+}
+__device__ __forceinline__ bool any_fluid(const uint16_t (&cc)[4]) {
+    return ((cc[0] | cc[1] | cc[2] | cc[3]) & CODE_FLUID) != 0;
+}
+
+// a field around a quad: centre and the four face-neighbour quads, plus z ends
+struct Q7 {
+    float c[4], xp[4], xm[4], yp[4], ym[4];
+    float zm, zp;
+};
+// neighbour quads outside the level read as zero (their mask bits are clear)
+__device__ __forceinline__ void load_q7(Q7& q, const float* v, long long c0, const MGLev& L, int x, int y, int z0) {
+    const long long sx = (long long)L.pz * L.ny, sy = L.pz;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    unpack4(ld4(v + c0), q.c);
+    unpack4(x + 1 < L.nx ? ld4(v + c0 + sx) : zero, q.xp);
+    unpack4(x > 0 ? ld4(v + c0 - sx) : zero, q.xm);
+    unpack4(y + 1 < L.ny ? ld4(v + c0 + sy) : zero, q.yp);
+    unpack4(y > 0 ? ld4(v + c0 - sy) : zero, q.ym);
+    q.zm = z0 > 0 ? v[c0 - 1] : 0.f;
+    q.zp = z0 + 4 < L.pz ? v[c0 + 4] : 0.f;
+}
+__device__ __forceinline__ void codes4_nb(const uint16_t* code, long long c0, bool ok, uint16_t (&cc)[4]) {
+    if (ok) codes4(code, c0, cc);
+    else cc[0] = cc[1] = cc[2] = cc[3] = 0;
+}
+// sum over the fluid neighbours (mask bits of cc) of lane i
+__device__ __forceinline__ float nbsum(const Q7& q, int i, uint16_t cc) {
+    float s = 0.f;
+    if (cc & 1) s += q.xp[i];
+    if (cc & 2) s += q.xm[i];
+    if (cc & 4) s += q.yp[i];
+    if (cc & 8) s += q.ym[i];
+    if (cc & 16) s += (i < 3) ? q.c[i + 1] : q.zp;
+    if (cc & 32) s += (i > 0) ? q.c[i - 1] : q.zm;
+    return s;
+}
+
 template <bool FINE, typename F>
-__device__ __forceinline__ void mg_for_cells(const PcgArgs& A, const MGLev& L, F&& fn) {
+__device__ __forceinline__ void mg_for_quads(const PcgArgs& A, const MGLev& L, F&& fn) {
     if (FINE) {
         const int nact = *A.nactive;
-        for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
-            int x, y, z;
-            long long c;
-            if (brick_cell(A.B, A.list[bk], threadIdx.x, x, y, z, c)) fn(x, y, z, c);
+        const int sub = threadIdx.x >> 6, q = threadIdx.x & 63;
+        for (int bk = blockIdx.x * 4 + sub; bk < nact; bk += gridDim.x * 4) {
+            const int b = A.list[bk];
+            const int bz = b % A.B.nbz, by = (b / A.B.nbz) % A.B.nby, bx = b / (A.B.nbz * A.B.nby);
+            const int x = bx * BRX + (q >> 5), y = by * BRY + ((q >> 3) & 3), z0 = bz * BRZ + ((q & 7) << 2);
+            if (x >= L.nx || y >= L.ny || z0 >= L.nz) continue;
+            fn(x, y, z0, ((long long)x * L.ny + y) * L.pz + z0);
         }
     } else {
-        const long long n = (long long)L.nx * L.ny * L.nz;
+        const int qz = L.pz >> 2;
+        const long long n = (long long)L.nx * L.ny * qz;
         for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
              i += (long long)gridDim.x * blockDim.x) {
-            const int z = (int)(i % L.nz);
-            const long long t = i / L.nz;
+            const int z0 = (int)(i % qz) << 2;
+            const long long t = i / qz;
             const int y = (int)(t % L.ny), x = (int)(t / L.ny);
-            fn(x, y, z, ((long long)x * L.ny + y) * L.pz + z);
+            fn(x, y, z0, ((long long)x * L.ny + y) * L.pz + z0);
         }
     }
 }
+
+__device__ __forceinline__ long long lev_sx(const MGLev& L) { return (long long)L.pz * L.ny; }
 
 // one red-black Gauss-Seidel half sweep; first: the other colour is still zero
 template <bool FINE>
 __global__ void __launch_bounds__(PCG_THREADS) k_mg_smooth(const PcgArgs A, MGLev L, int color, int first) {
     if (A.st->done) return;
     const float* rhs = mg_rhs(A, L);
-    mg_for_cells<FINE>(A, L, [&](int x, int y, int z, long long c) {
-        if (((x + y + z) & 1) != color) return;
-        const uint16_t cc = L.code[c];
-        if (!(cc & CODE_FLUID)) return;
-        float sum = rhs[c];
-        if (!first) {
+    mg_for_quads<FINE>(A, L, [&](int x, int y, int z0, long long c0) {
+        uint16_t cc[4];
+        codes4(L.code, c0, cc);
+        if (!any_fluid(cc)) return;
+        float f[4];
+        unpack4(ld4(rhs + c0), f);
+        Q7 q;
+        if (first) unpack4(ld4(L.x + c0), q.c);
+        else load_q7(q, L.x, c0, L, x, y, z0);
+        const int par = (x + y + z0) & 1;
+        float out[4] = {q.c[0], q.c[1], q.c[2], q.c[3]};
 #pragma unroll
-            for (int k = 0; k < 6; k++)
-                if ((cc >> k) & 1) sum += L.x[c + mg_off(L, k)];
+        for (int i = 0; i < 4; i++) {
+            if (((par ^ i) & 1) != color || !(cc[i] & CODE_FLUID)) continue;
+            float sum = f[i];
+            if (!first) sum += nbsum(q, i, cc[i]);
+            out[i] = sum * c_rcp[code_ns(cc[i])];
         }
-        L.x[c] = sum * c_rcp[code_ns(cc)];
+        st4(L.x + c0, out);
     });
 }
 
-// the last post-smoothing half sweep (red, level 0) fused with z.r (modes as k_red)
+// the last post-smoothing half sweep (red, level 0) fused with z.r (modes 0/1 as k_red)
 __global__ void __launch_bounds__(PCG_THREADS) k_mg_smooth_dot(const PcgArgs A, MGLev L, int mode) {
     __shared__ double scratch[32];
     if (A.st->done) return;
     const float* rhs = mg_rhs(A, L);
     Acc<float> zr;
-    mg_for_cells<true>(A, L, [&](int x, int y, int z, long long c) {
-        const uint16_t cc = L.code[c];
-        if (!(cc & CODE_FLUID)) return;
-        const float rv = rhs[c];
-        float zv;
-        if (((x + y + z) & 1) == 0) {
-            float sum = rv;
+    mg_for_quads<true>(A, L, [&](int x, int y, int z0, long long c0) {
+        uint16_t cc[4];
+        codes4(L.code, c0, cc);
+        if (!any_fluid(cc)) return;
+        float f[4];
+        unpack4(ld4(rhs + c0), f);
+        Q7 q;
+        load_q7(q, L.x, c0, L, x, y, z0);
+        const int par = (x + y + z0) & 1;
+        float out[4] = {q.c[0], q.c[1], q.c[2], q.c[3]};
 #pragma unroll
-            for (int k = 0; k < 6; k++)
-                if ((cc >> k) & 1) sum += L.x[c + mg_off(L, k)];
-            zv = sum * c_rcp[code_ns(cc)];
-            L.x[c] = zv;
-        } else {
-            zv = L.x[c];
+        for (int i = 0; i < 4; i++) {
+            if (!(cc[i] & CODE_FLUID)) continue;
+            if (((par ^ i) & 1) == 0) out[i] = (f[i] + nbsum(q, i, cc[i])) * c_rcp[code_ns(cc[i])];
+            zr.add(out[i] * f[i]);
         }
-        zr.add(zv * rv);
+        st4(L.x + c0, out);
     });
     double acc[1] = {zr.value()};
     if (last_block_reduce<1>(acc, 0, A.partials, A.counter, scratch)) {
@@ -630,28 +663,38 @@ template <bool FINE>
 __global__ void __launch_bounds__(PCG_THREADS) k_mg_residual(const PcgArgs A, MGLev L) {
     if (A.st->done) return;
     const float* rhs = mg_rhs(A, L);
-    mg_for_cells<FINE>(A, L, [&](int x, int y, int z, long long c) {
-        const uint16_t cc = L.code[c];
-        if (!(cc & CODE_FLUID)) return;
-        float ax = (float)code_ns(cc) * L.x[c];
+    mg_for_quads<FINE>(A, L, [&](int x, int y, int z0, long long c0) {
+        uint16_t cc[4];
+        codes4(L.code, c0, cc);
+        if (!any_fluid(cc)) return;
+        float f[4];
+        unpack4(ld4(rhs + c0), f);
+        Q7 q;
+        load_q7(q, L.x, c0, L, x, y, z0);
+        float out[4];
 #pragma unroll
-        for (int k = 0; k < 6; k++)
-            if ((cc >> k) & 1) ax -= L.x[c + mg_off(L, k)];
-        L.r[c] = rhs[c] - ax;
+        for (int i = 0; i < 4; i++)
+            out[i] = (cc[i] & CODE_FLUID) ? f[i] - ((float)code_ns(cc[i]) * q.c[i] - nbsum(q, i, cc[i])) : 0.f;
+        st4(L.r + c0, out);
     });
 }
 
-// coarse f = 0.5 * sum_fine P[f,C] r_f  (= 4 R r); coarse cells, dense
+// coarse f = 0.5 * sum_fine P[f,C] r_f  (= 4 R r), per coarse quad:
+// fine z 2 z0 - 1 .. 2 z0 + 8 come from the four fine quads at 2 z0 - 4 .. 2 z0 + 8
 __global__ void __launch_bounds__(PCG_THREADS) k_mg_restrict(const PcgState* st, MGLev F, MGLev Cl) {
     if (st->done) return;
-    const long long n = (long long)Cl.nx * Cl.ny * Cl.nz;
+    const int qz = Cl.pz >> 2;
+    const long long n = (long long)Cl.nx * Cl.ny * qz;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int cz = (int)(i % Cl.nz);
-        const long long t = i / Cl.nz;
+        const int cz0 = (int)(i % qz) << 2;
+        const long long t = i / qz;
         const int cy = (int)(t % Cl.ny), cx = (int)(t / Cl.ny);
-        const long long cidx = ((long long)cx * Cl.ny + cy) * Cl.pz + cz;
-        if (!(Cl.code[cidx] & CODE_FLUID)) continue;
-        float sum = 0.f;
+        const long long ci = ((long long)cx * Cl.ny + cy) * Cl.pz + cz0;
+        uint16_t ccc[4];
+        codes4(Cl.code, ci, ccc);
+        if (!any_fluid(ccc)) continue;
+        float sum[4] = {0.f, 0.f, 0.f, 0.f};
+        const int fz0 = 2 * cz0 - 4;  // first fine z loaded (a multiple of 4)
         for (int dx = -1; dx <= 2; dx++) {
             const int fx = 2 * cx + dx;
             if (fx < 0 || fx >= F.nx) continue;
@@ -661,42 +704,221 @@ __global__ void __launch_bounds__(PCG_THREADS) k_mg_restrict(const PcgState* st,
                 if (fy < 0 || fy >= F.ny) continue;
                 const float wxy = wx * ((dy == 0 || dy == 1) ? 0.75f : 0.25f);
                 const long long row = ((long long)fx * F.ny + fy) * F.pz;
+                // 16 fine values z = fz0 .. fz0 + 15, masked by fine fluid
+                float fr[16];
 #pragma unroll
-                for (int dz = -1; dz <= 2; dz++) {
-                    const int fz = 2 * cz + dz;
-                    if (fz < 0 || fz >= F.nz) continue;
-                    if (!(F.code[row + fz] & CODE_FLUID)) continue;
-                    sum += wxy * ((dz == 0 || dz == 1) ? 0.75f : 0.25f) * F.r[row + fz];
+                for (int k = 0; k < 4; k++) {
+                    const int z = fz0 + 4 * k;
+                    float v[4] = {0.f, 0.f, 0.f, 0.f};
+                    if (z >= 0 && z < F.pz) {
+                        uint16_t fc[4];
+                        codes4(F.code, row + z, fc);
+                        if (any_fluid(fc)) {
+                            unpack4(ld4(F.r + row + z), v);
+#pragma unroll
+                            for (int e = 0; e < 4; e++)
+                                if (!(fc[e] & CODE_FLUID)) v[e] = 0.f;
+                        }
+                    }
+#pragma unroll
+                    for (int e = 0; e < 4; e++) fr[4 * k + e] = v[e];
                 }
+                // coarse lane j takes fine 2(cz0+j) - 1 .. 2(cz0+j) + 2 = fr[3 + 2j .. 6 + 2j]
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    sum[j] += wxy * (0.25f * fr[3 + 2 * j] + 0.75f * fr[4 + 2 * j] + 0.75f * fr[5 + 2 * j] +
+                                     0.25f * fr[6 + 2 * j]);
             }
         }
-        const_cast<float*>(Cl.f)[cidx] = 0.5f * sum;
+        float out[4];
+        unpack4(ld4(Cl.f + ci), out);
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (ccc[j] & CODE_FLUID) out[j] = 0.5f * sum[j];
+        st4(const_cast<float*>(Cl.f) + ci, out);
     }
 }
 
-// fine x += P x_coarse on fluid fine cells
+// fine x += P x_coarse on fluid fine cells, per fine quad: the quad's coarse z
+// neighbours are z0/2 - 1 .. z0/2 + 2
 template <bool FINE>
 __global__ void __launch_bounds__(PCG_THREADS) k_mg_prolong(const PcgArgs A, MGLev F, MGLev Cl) {
     if (A.st->done) return;
-    mg_for_cells<FINE>(A, F, [&](int x, int y, int z, long long c) {
-        if (!(F.code[c] & CODE_FLUID)) return;
+    mg_for_quads<FINE>(A, F, [&](int x, int y, int z0, long long c0) {
+        uint16_t cc[4];
+        codes4(F.code, c0, cc);
+        if (!any_fluid(cc)) return;
         const int px = (x & 1) ? x >> 1 : (x >> 1) - 1;  // lower coarse neighbour per axis
         const int py = (y & 1) ? y >> 1 : (y >> 1) - 1;
-        const int pz = (z & 1) ? z >> 1 : (z >> 1) - 1;
-        const float wlx = (x & 1) ? 0.75f : 0.25f, wly = (y & 1) ? 0.75f : 0.25f, wlz = (z & 1) ? 0.75f : 0.25f;
-        float sum = 0.f;
+        const float wlx = (x & 1) ? 0.75f : 0.25f, wly = (y & 1) ? 0.75f : 0.25f;
+        const int zc = (z0 >> 1) - 1;
+        float sum[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int o = 0; o < 8; o++) {
-            const int ox = o >> 2, oy = (o >> 1) & 1, oz = o & 1;
-            const int cx = px + ox, cy = py + oy, cz = pz + oz;
-            if (cx < 0 || cy < 0 || cz < 0 || cx >= Cl.nx || cy >= Cl.ny || cz >= Cl.nz) continue;
-            const long long ci = ((long long)cx * Cl.ny + cy) * Cl.pz + cz;
-            if (!(Cl.code[ci] & CODE_FLUID)) continue;
-            const float w = (ox ? 1.f - wlx : wlx) * (oy ? 1.f - wly : wly) * (oz ? 1.f - wlz : wlz);
-            sum += w * Cl.x[ci];
+        for (int o = 0; o < 4; o++) {
+            const int ox = o >> 1, oy = o & 1;
+            const int cx = px + ox, cy = py + oy;
+            if (cx < 0 || cy < 0 || cx >= Cl.nx || cy >= Cl.ny) continue;
+            const float wxy = (ox ? 1.f - wlx : wlx) * (oy ? 1.f - wly : wly);
+            const long long row = ((long long)cx * Cl.ny + cy) * Cl.pz;
+            float cv[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int z = zc + k;
+                cv[k] = (z >= 0 && z < Cl.nz && (Cl.code[row + z] & CODE_FLUID)) ? Cl.x[row + z] : 0.f;
+            }
+            // lanes: z0 (lower zc, w 1/4), z0+1 (zc+1, 3/4), z0+2 (zc+1, 1/4), z0+3 (zc+2, 3/4)
+            sum[0] += wxy * (0.25f * cv[0] + 0.75f * cv[1]);
+            sum[1] += wxy * (0.75f * cv[1] + 0.25f * cv[2]);
+            sum[2] += wxy * (0.25f * cv[1] + 0.75f * cv[2]);
+            sum[3] += wxy * (0.75f * cv[2] + 0.25f * cv[3]);
         }
-        F.x[c] += sum;
+        float xv[4];
+        unpack4(ld4(F.x + c0), xv);
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+            if (cc[i] & CODE_FLUID) xv[i] += sum[i];
+        st4(F.x + c0, xv);
     });
+}
+
+// ---- MG-path PCG kernels on quads (level 0, FP32) ------------------------------
+// s_new = z + beta s_old; q = A' s_new; alpha = sigma / (s.q)
+__global__ void __launch_bounds__(PCG_THREADS) k_spmv_q(const PcgArgs a, Vecs<float> v, MGLev L) {
+    __shared__ double scratch[32];
+    if (a.st->done) return;
+    const int sc = (a.st->bufsel >> 1) & 1;
+    const float beta = (float)a.st->beta;
+    const float* so = sc ? v.s[1] : v.s[0];
+    float* sn = sc ? v.s[0] : v.s[1];
+    Acc<float> sq;
+    mg_for_quads<true>(a, L, [&](int x, int y, int z0, long long c0) {
+        uint16_t cc[4];
+        codes4(a.code, c0, cc);
+        if (!any_fluid(cc)) return;
+        Q7 zq, sq7;
+        load_q7(zq, v.z, c0, L, x, y, z0);
+        load_q7(sq7, so, c0, L, x, y, z0);
+        Q7 n;  // s_new around the quad
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            n.c[i] = zq.c[i] + beta * sq7.c[i];
+            n.xp[i] = zq.xp[i] + beta * sq7.xp[i];
+            n.xm[i] = zq.xm[i] + beta * sq7.xm[i];
+            n.yp[i] = zq.yp[i] + beta * sq7.yp[i];
+            n.ym[i] = zq.ym[i] + beta * sq7.ym[i];
+        }
+        n.zm = zq.zm + beta * sq7.zm;
+        n.zp = zq.zp + beta * sq7.zp;
+        float qv[4], snc[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            if (cc[i] & CODE_FLUID) {
+                snc[i] = n.c[i];
+                qv[i] = (float)code_ns(cc[i]) * n.c[i] - nbsum(n, i, cc[i]);
+                sq.add(snc[i] * qv[i]);
+            } else {
+                snc[i] = 0.f;
+                qv[i] = 0.f;
+            }
+        }
+        st4(sn + c0, snc);
+        st4(v.q + c0, qv);
+    });
+    double acc[1] = {sq.value()};
+    if (last_block_reduce<1>(acc, 0, a.partials, a.counter, scratch)) {
+        if (threadIdx.x == 0) {
+            PcgState* s = a.st;
+            s->alpha = s->sigma / acc[0];
+            if (!isfinite(s->alpha)) {
+                s->nan = 1;
+                s->done = 1;
+            }
+            s->bufsel ^= 2;
+        }
+    }
+}
+
+// x += alpha s; r_new = r - alpha q; r.r, max|r|; first red-black sweep of the
+// V-cycle from zero on r_new (red z = r/ns, black z = (r + sum_j r_j/ns_j)/ns)
+__global__ void __launch_bounds__(PCG_THREADS) k_update_q(const PcgArgs a, Vecs<float> v, MGLev L) {
+    __shared__ double scratch[32 * 2];
+    if (a.st->done) return;
+    const int rc = a.st->bufsel & 1, sc = (a.st->bufsel >> 1) & 1;
+    const float alpha = (float)a.st->alpha;
+    const float* ro = rc ? v.r[1] : v.r[0];
+    float* rn = rc ? v.r[0] : v.r[1];
+    const float* s = sc ? v.s[1] : v.s[0];
+    const long long sx = lev_sx(L), sy = L.pz;
+    Acc<float> rr;
+    float rmax = 0.f;
+    mg_for_quads<true>(a, L, [&](int x, int y, int z0, long long c0) {
+        uint16_t cc[4];
+        codes4(a.code, c0, cc);
+        if (!any_fluid(cc)) return;
+        float sv[4], xv[4];
+        unpack4(ld4(s + c0), sv);
+        unpack4(ld4(v.x + c0), xv);
+        Q7 rq, qq;
+        load_q7(rq, ro, c0, L, x, y, z0);
+        load_q7(qq, v.q, c0, L, x, y, z0);
+        // neighbour codes for their 1/ns
+        uint16_t cxp[4], cxm[4], cyp[4], cym[4];
+        codes4_nb(a.code, c0 + sx, x + 1 < L.nx, cxp);
+        codes4_nb(a.code, c0 - sx, x > 0, cxm);
+        codes4_nb(a.code, c0 + sy, y + 1 < L.ny, cyp);
+        codes4_nb(a.code, c0 - sy, y > 0, cym);
+        const uint16_t czm = z0 > 0 ? a.code[c0 - 1] : 0, czp = z0 + 4 < L.pz ? a.code[c0 + 4] : 0;
+        Q7 w;  // r_new / ns around the quad
+        float rnc[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            rnc[i] = rq.c[i] - alpha * qq.c[i];
+            w.c[i] = rnc[i] * c_rcp[code_ns(cc[i])];
+            w.xp[i] = (rq.xp[i] - alpha * qq.xp[i]) * c_rcp[code_ns(cxp[i])];
+            w.xm[i] = (rq.xm[i] - alpha * qq.xm[i]) * c_rcp[code_ns(cxm[i])];
+            w.yp[i] = (rq.yp[i] - alpha * qq.yp[i]) * c_rcp[code_ns(cyp[i])];
+            w.ym[i] = (rq.ym[i] - alpha * qq.ym[i]) * c_rcp[code_ns(cym[i])];
+        }
+        w.zm = (rq.zm - alpha * qq.zm) * c_rcp[code_ns(czm)];
+        w.zp = (rq.zp - alpha * qq.zp) * c_rcp[code_ns(czp)];
+        const int par = (x + y + z0) & 1;
+        float zv[4], rout[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            if (!(cc[i] & CODE_FLUID)) {
+                zv[i] = 0.f;
+                rout[i] = 0.f;
+                continue;
+            }
+            xv[i] += alpha * sv[i];
+            rout[i] = rnc[i];
+            rr.add(rnc[i] * rnc[i]);
+            rmax = fmaxf(rmax, fabsf(rnc[i]));
+            if (((par ^ i) & 1) == 0) zv[i] = w.c[i];  // red
+            else zv[i] = (rnc[i] + nbsum(w, i, cc[i])) * c_rcp[code_ns(cc[i])];
+        }
+        st4(v.x + c0, xv);
+        st4(rn + c0, rout);
+        st4(v.z + c0, zv);
+    });
+    double acc[2] = {rr.value(), (double)rmax};
+    if (last_block_reduce<2>(acc, 0x2, a.partials, a.counter, scratch)) {
+        if (threadIdx.x == 0) {
+            PcgState* st = a.st;
+            st->rr = acc[0];
+            st->rmax = acc[1];
+            st->it += 1;
+            st->bufsel ^= 1;
+            const bool conv = (st->tol_mode == FSIM_TOL_ABS_MAX) ? (acc[1] < st->tol_abs) : (acc[0] <= st->tol_rel2);
+            st->converged = conv ? 1 : 0;
+            if (conv || st->it >= st->max_iters || !isfinite(acc[0])) st->done = 1;
+            if (!isfinite(acc[0])) st->nan = 1;
+            if (st->fold_enabled && acc[0] < 0.01 * st->rr_update) {
+                st->need_fold = 1;
+                st->done = 1;
+            }
+        }
+    }
 }
 
 // coarsest level: symmetric red-black Gauss-Seidel in shared memory, one CTA
@@ -705,11 +927,12 @@ __global__ void __launch_bounds__(1024) k_mg_bottom(const PcgState* st, MGLev L)
     __shared__ float sx[MG_BOTTOM_MAX];
     __shared__ float sf[MG_BOTTOM_MAX];
     __shared__ uint16_t sc[MG_BOTTOM_MAX];
-    const int n = L.nx * L.ny * L.nz;  // dense (pz == nz)
+    const int n = L.nx * L.ny * L.nz;  // dense in shared memory, padded in global
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const long long gi = (long long)(i / L.nz) * L.pz + (i % L.nz);
         sx[i] = 0.f;
-        sf[i] = L.f[i];
-        sc[i] = L.code[i];
+        sf[i] = L.f[gi];
+        sc[i] = L.code[gi];
     }
     __syncthreads();
     const int sxs = L.ny * L.nz, sys = L.nz;
@@ -734,7 +957,7 @@ __global__ void __launch_bounds__(1024) k_mg_bottom(const PcgState* st, MGLev L)
             __syncthreads();
         }
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) L.x[i] = sx[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) L.x[(long long)(i / L.nz) * L.pz + (i % L.nz)] = sx[i];
 }
 
 // coarse cell kinds: fluid if any child is fluid, else air if any child is air
@@ -745,6 +968,7 @@ __global__ void k_mg_coarsen(MGLev F, const uint8_t* fkind, const uint8_t* fflag
     const int cz = (int)(i % Cl.nz);
     const long long t = i / Cl.nz;
     const int cy = (int)(t % Cl.ny), cx = (int)(t / Cl.ny);
+    const long long ci = ((long long)cx * Cl.ny + cy) * Cl.pz + cz;
     int best = 2;
     for (int o = 0; o < 8; o++) {
         const int fx = 2 * cx + (o >> 2), fy = 2 * cy + ((o >> 1) & 1), fz = 2 * cz + (o & 1);
@@ -755,7 +979,7 @@ __global__ void k_mg_coarsen(MGLev F, const uint8_t* fkind, const uint8_t* fflag
         else k = (F.code[fi] & CODE_FLUID) ? 0 : (fflags[fi] == C_AIR ? 1 : 2);
         best = min(best, k);
     }
-    ckind[i] = (uint8_t)best;
+    ckind[ci] = (uint8_t)best;
 }
 
 // per-cell code of a coarse level from its kinds (outside the level = solid)
@@ -766,8 +990,9 @@ __global__ void k_mg_code(MGLev L, const uint8_t* kind, uint16_t* code) {
     const int z = (int)(i % L.nz);
     const long long t = i / L.nz;
     const int y = (int)(t % L.ny), x = (int)(t / L.ny);
-    if (kind[i] != 0) {
-        code[i] = 0;
+    const long long ci = ((long long)x * L.ny + y) * L.pz + z;
+    if (kind[ci] != 0) {
+        code[ci] = 0;
         return;
     }
     uint16_t cd = CODE_FLUID;
@@ -778,11 +1003,11 @@ __global__ void k_mg_code(MGLev L, const uint8_t* kind, uint16_t* code) {
         const int a = k >> 1, dir = (k & 1) ? -1 : 1;
         const int q = pos[a] + dir;
         if (q < 0 || q >= lim[a]) continue;
-        const uint8_t kn = kind[i + mg_off(L, k)];
+        const uint8_t kn = kind[ci + mg_off(L, k)];
         if (kn == 0) cd |= (uint16_t)(1u << k);
         if (kn != 2) ns++;
     }
-    code[i] = cd | (uint16_t)(ns << 8);
+    code[ci] = cd | (uint16_t)(ns << 8);
 }
 
 // phi += x; x = 0   (fold the FP32 accumulator into the FP64 solution)
@@ -816,6 +1041,7 @@ int solver_alloc(fsim_ctx* ctx) {
     FSIM_CUDA_TRY(ctx, cudaMalloc(&S.d_nactive, sizeof(int)));
     FSIM_CUDA_TRY(ctx, cudaMalloc(&S.brick_flag, S.nbricks));
     FSIM_CUDA_TRY(ctx, cudaMalloc(&S.code, nc * sizeof(uint16_t)));
+    FSIM_CUDA_TRY(ctx, cudaMemset(S.code, 0, nc * sizeof(uint16_t)));
     FSIM_CUDA_TRY(ctx, cudaMalloc(&S.b, nc * sizeof(double)));
     FSIM_CUDA_TRY(ctx, cudaMalloc(&S.phi, nc * sizeof(double)));
     FSIM_CUDA_TRY(ctx, cudaMemset(S.phi, 0, nc * sizeof(double)));
@@ -843,26 +1069,31 @@ int solver_alloc(fsim_ctx* ctx) {
     float rcp[7];
     for (int ns = 0; ns < 7; ns++) rcp[ns] = ns > 0 ? 1.f / ns : 1.f;
     FSIM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rcp, rcp, sizeof(rcp)));
-    // multigrid hierarchy: halve until every dimension is <= 8
+    // multigrid hierarchy: halve until every dimension is <= 4
     MGLevelBufs l0;
     l0.nx = g.nx; l0.ny = g.ny; l0.nz = g.nz; l0.pz = g.pz; l0.ncell = g.ncell;
     l0.code = S.code;
     FSIM_CUDA_TRY(ctx, cudaMalloc(&l0.r, nc * sizeof(float)));
+    FSIM_CUDA_TRY(ctx, cudaMemset(l0.r, 0, nc * sizeof(float)));
     S.mg.push_back(l0);
-    while (std::max(S.mg.back().nx, std::max(S.mg.back().ny, S.mg.back().nz)) > 8) {
+    while (std::max(S.mg.back().nx, std::max(S.mg.back().ny, S.mg.back().nz)) > 4) {
         const MGLevelBufs& f = S.mg.back();
         MGLevelBufs c;
-        c.nx = (f.nx + 1) / 2; c.ny = (f.ny + 1) / 2; c.nz = (f.nz + 1) / 2; c.pz = c.nz;
-        c.ncell = (long long)c.nx * c.ny * c.nz;
+        c.nx = (f.nx + 1) / 2; c.ny = (f.ny + 1) / 2; c.nz = (f.nz + 1) / 2; c.pz = (c.nz + 3) & ~3;
+        c.ncell = (long long)c.nx * c.ny * c.pz;
         FSIM_CUDA_TRY(ctx, cudaMalloc(&c.kind, c.ncell));
         FSIM_CUDA_TRY(ctx, cudaMalloc(&c.code, c.ncell * sizeof(uint16_t)));
         FSIM_CUDA_TRY(ctx, cudaMalloc(&c.x, c.ncell * sizeof(float)));
         FSIM_CUDA_TRY(ctx, cudaMalloc(&c.f, c.ncell * sizeof(float)));
         FSIM_CUDA_TRY(ctx, cudaMalloc(&c.r, c.ncell * sizeof(float)));
         FSIM_CUDA_TRY(ctx, cudaMemset(c.x, 0, c.ncell * sizeof(float)));
+        FSIM_CUDA_TRY(ctx, cudaMemset(c.f, 0, c.ncell * sizeof(float)));
+        FSIM_CUDA_TRY(ctx, cudaMemset(c.r, 0, c.ncell * sizeof(float)));
+        FSIM_CUDA_TRY(ctx, cudaMemset(c.code, 0, c.ncell * sizeof(uint16_t)));
+        FSIM_CUDA_TRY(ctx, cudaMemset(c.kind, 2, c.ncell));
         S.mg.push_back(c);
     }
-    if (S.mg.back().ncell > MG_BOTTOM_MAX) {
+    if ((long long)S.mg.back().nx * S.mg.back().ny * S.mg.back().nz > MG_BOTTOM_MAX) {
         ctx->err = "multigrid coarsest level too large";
         return FSIM_E_INVALID;
     }
@@ -961,6 +1192,7 @@ void solver_free(fsim_ctx* ctx) {
     cudaFree(S.brick_list); cudaFree(S.d_nactive); cudaFree(S.brick_flag); cudaFree(S.code);
     cudaFree(S.b); cudaFree(S.phi); cudaFree(S.r); cudaFree(S.r64); cudaFree(S.partials);
     cudaFree(S.counter); cudaFree(S.st); cudaFreeHost(S.st_host); cudaFree(S.guess);
+    if (S.iter_exec) cudaGraphExecDestroy(S.iter_exec);
     for (size_t l = 0; l < S.mg.size(); l++) {
         cudaFree(S.mg[l].r);
         if (l > 0) {
@@ -1006,15 +1238,45 @@ static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, int prec
     fsim_record(ctx, EV_PCG_SETUP);
     int rc = read_state();
     if (rc) return rc;
+    // one iteration as a CUDA graph (captured once per context and configuration;
+    // every kernel reads its varying scalars from the device state)
+    auto enqueue_iteration = [&]() {
+        if (mg) {
+            const MGLev L0 = mg_lev(S, 0, nullptr, nullptr, nullptr);
+            Vecs<float> vf = *reinterpret_cast<Vecs<float>*>(&v);
+            k_spmv_q<<<G, PCG_THREADS, 0, st>>>(A, vf, L0);
+            k_update_q<<<G, PCG_THREADS, 0, st>>>(A, vf, L0);
+        } else {
+            k_spmv<T><<<G, PCG_THREADS, 0, st>>>(A, v);
+            k_update<T, 1><<<G, PCG_THREADS, 0, st>>>(A, v);
+        }
+        ctx->launches += 2;
+        precondition(1, true);
+    };
+    const int key = (int)sizeof(T) * 1000 + (mg ? 100 : 0) + ctx->prm.mg_sweeps;
+    if (S.iter_exec == nullptr || S.iter_key != key) {
+        if (S.iter_exec) {
+            cudaGraphExecDestroy(S.iter_exec);
+            S.iter_exec = nullptr;
+        }
+        const long long l0 = ctx->launches;
+        cudaGraph_t graph = nullptr;
+        FSIM_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        enqueue_iteration();
+        FSIM_CUDA_TRY(ctx, cudaStreamEndCapture(st, &graph));
+        cudaError_t ie = cudaGraphInstantiate(&S.iter_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        FSIM_CUDA_TRY(ctx, ie);
+        S.iter_key = key;
+        S.iter_kernels = (int)(ctx->launches - l0);
+        ctx->launches = l0;
+    }
     int chunk = mg ? 2 : 4;
     const int chunk_max = mg ? 8 : 16;
     while (!S.st_host->done && !S.st_host->nan) {
         for (int k = 0; k < chunk; k++) {
-            k_spmv<T><<<G, PCG_THREADS, 0, st>>>(A, v);
-            if (mg) k_update<T, 2><<<G, PCG_THREADS, 0, st>>>(A, v);
-            else k_update<T, 1><<<G, PCG_THREADS, 0, st>>>(A, v);
-            ctx->launches += 2;
-            precondition(1, true);
+            FSIM_CUDA_TRY(ctx, cudaGraphLaunch(S.iter_exec, st));
+            ctx->launches += S.iter_kernels;
         }
         if ((rc = read_state())) return rc;
         if (chunk < chunk_max) chunk *= 2;

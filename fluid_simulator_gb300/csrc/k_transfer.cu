@@ -26,10 +26,7 @@
 namespace {
 
 constexpr int TX = 8, TY = 8, TZ = 32;
-constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2;
-constexpr int TCELLS = TX * TY * TZ;
 constexpr int P2G_THREADS = 256;
-constexpr int P2G_SMEM = 7 * TCELLS * (int)sizeof(float);
 
 // G2P staged box: x in [x0-1, x0+TX], y in [y0-1, y0+TY], z in [z0-4, z0+TZ+4)
 constexpr int BX = TX + 2, BY = TY + 2, BZ = TZ + 8;
@@ -47,98 +44,177 @@ struct P2GArgs {
     int ntx, nty, ntz;
 };
 
+// P2G tile (owned cells) and its one-cell halo
+constexpr int PX = 12, PY = 16, PZ = 32;
+constexpr int QX = PX + 2, QY = PY + 2, QZ = PZ + 2;
+constexpr int PCELLS = PX * PY * PZ;
+constexpr int P2G_SMEM_V2 = 7 * PCELLS * (int)sizeof(float);  // 172,032 B
+
+// 1D tent weights of the three cell-centred nodes at relative -0.5, 0.5, 1.5
+// (f = position in the cell, 0 <= f < 1): the two nodes the reference's
+// trunc-based stencil picks get 1 - |f - node|, the third gets 0.
+__device__ __forceinline__ void tent3(float f, float (&w)[3]) {
+    w[0] = fmaxf(0.f, 0.5f - f);
+    w[1] = 1.f - fabsf(f - 0.5f);
+    w[2] = fmaxf(0.f, f - 0.5f);
+}
+
+// Warps come in pairs over blocks of 32 consecutive tile+halo cells (one cell
+// per lane).  The even warp of a pair handles the x faces and the cell-centre
+// density of its cells, the odd warp the y and z faces; both walk the same
+// particles at the same time, so the second reads hit L1.  Each lane walks its
+// cell's particles once and accumulates, in registers, the full 2x3x3 face
+// stencil of its axes (faces of the cells at normal offset -1, 0 and
+// transverse offsets -1, 0, +1: the union of getFacesAround's 8-face stencils
+// over the cell) and the 3x3x3 stencil of getCellsAround -- the merged
+// contribution of all particles of the cell.  It then adds the entries inside
+// the tile to the tile's shared accumulators (lanes hold distinct cells, so a
+// warp's adds never collide).
+constexpr int P2G_THREADS_V2 = 384;
+
+// accumulators of one lane: role 0 uses [0,18) weights x, [18,36) values x,
+// [36,63) density; role 1 uses [0,18)/[18,36) for y and [36,54)/[54,72) for z
+constexpr int NACC = 72;
+
+template <bool APIC, int AX, int OW, int OV>
+__device__ __forceinline__ void p2g_face_axis(const float (&f)[3], const float (&wt)[3][3], float va,
+                                              const float* cm, float h, float (&acc)[NACC]) {
+    constexpr int b = AX == 0 ? 1 : 0, c = AX == 2 ? 1 : 2;  // transverse axes, increasing
+    const float wn[2] = {1.f - f[AX], f[AX]};
+    float K = va, ka = 0.f, kb = 0.f, kc = 0.f;
+    if (APIC) {
+        // contribution v_a + c[a] . (face - pos) = K + h (c_a ii + c_b (j - 1/2) + c_c (k - 1/2))
+        K -= h * (cm[0] * f[0] + cm[1] * f[1] + cm[2] * f[2]);
+        ka = h * cm[AX];
+        kb = h * cm[b];
+        kc = h * cm[c];
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int kk = 0; kk < 3; kk++) {
+            const float wbc = wt[b][j] * wt[c][kk];
+            const float cbc = K + kb * ((float)j - 0.5f) + kc * ((float)kk - 0.5f);
+#pragma unroll
+            for (int ii = 0; ii < 2; ii++) {
+                const float w = wn[ii] * wbc;
+                const int e = (ii * 3 + j) * 3 + kk;
+                acc[OW + e] += w;
+                acc[OV + e] += w * (APIC ? cbc + ka * (float)ii : K);
+            }
+        }
+}
+
+template <int AX, int OW, int OV>
+__device__ __forceinline__ void p2g_flush_axis(const float (&acc)[NACC], int cx, int cy, int cz, int x0, int y0,
+                                               int z0, float* s_vw, float* s_w) {
+    constexpr int b = AX == 0 ? 1 : 0, c = AX == 2 ? 1 : 2;
+#pragma unroll
+    for (int e = 0; e < 18; e++) {
+        if (acc[OW + e] == 0.f) continue;
+        int o[3];
+        o[AX] = e / 9 - 1;
+        o[b] = (e / 3) % 3 - 1;
+        o[c] = e % 3 - 1;
+        const int lx = cx + o[0] - x0, ly = cy + o[1] - y0, lz = cz + o[2] - z0;
+        if (lx < 0 || ly < 0 || lz < 0 || lx >= PX || ly >= PY || lz >= PZ) continue;
+        const int li = (lx * PY + ly) * PZ + lz;
+        atomicAdd(&s_vw[AX * PCELLS + li], acc[OV + e]);
+        atomicAdd(&s_w[AX * PCELLS + li], acc[OW + e]);
+    }
+}
+
 template <bool APIC>
-__global__ void __launch_bounds__(P2G_THREADS) k_p2g(const P2GArgs a) {
+__global__ void __launch_bounds__(P2G_THREADS_V2, 1) k_p2g(const P2GArgs a) {
     extern __shared__ float sm[];
-    float* s_vw = sm;              // [3][TCELLS] sum of w * contribution
-    float* s_w = sm + 3 * TCELLS;  // [3][TCELLS] sum of w
-    float* s_avg = sm + 6 * TCELLS;
-    for (int k = threadIdx.x; k < 7 * TCELLS; k += blockDim.x) sm[k] = 0.f;
+    float* s_vw = sm;              // [3][PCELLS] sum of w * contribution
+    float* s_w = sm + 3 * PCELLS;  // [3][PCELLS] sum of w
+    float* s_avg = sm + 6 * PCELLS;
+    for (int k = threadIdx.x; k < 7 * PCELLS; k += blockDim.x) sm[k] = 0.f;
     const int bt = blockIdx.x;
     const int tz = bt % a.ntz, ty = (bt / a.ntz) % a.nty, tx = bt / (a.ntz * a.nty);
-    const int x0 = tx * TX, y0 = ty * TY, z0 = tz * TZ;
+    const int x0 = tx * PX, y0 = ty * PY, z0 = tz * PZ;
     __syncthreads();
     const float hinv = a.g.hinv, h = a.g.h;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int role = warp & 1;                  // 0: x faces + density, 1: y and z faces
+    const int pairs = P2G_THREADS_V2 / 64;      // warp pairs per CTA
+    constexpr int HC = QX * QY * QZ;
 
-    for (int hc = threadIdx.x; hc < HX * HY * HZ; hc += blockDim.x) {
-        const int hz = hc % HZ, hy = (hc / HZ) % HY, hx = hc / (HZ * HY);
+    for (int blk = warp >> 1; blk * 32 < HC; blk += pairs) {
+        const int hc = blk * 32 + lane;
+        if (hc >= HC) continue;
+        const int hz = hc % QZ, hy = (hc / QZ) % QY, hx = hc / (QZ * QY);
         const int cx = x0 - 1 + hx, cy = y0 - 1 + hy, cz = z0 - 1 + hz;
         if (cx < 0 || cy < 0 || cz < 0 || cx >= a.g.nx || cy >= a.g.ny || cz >= a.g.nz) continue;
         const long long cell = gidx(a.g, cx, cy, cz);
         const int beg = a.cstart[cell], end = a.cstart[cell + 1];
+        if (beg == end) continue;
+        const int cc[3] = {cx, cy, cz};
+        float acc[NACC];
+#pragma unroll
+        for (int e = 0; e < NACC; e++) acc[e] = 0.f;
+
         for (int k = beg; k < end; k++) {
             const uint32_t i = a.perm[k];
-            const float g[3] = {a.p.p[0][i] * hinv, a.p.p[1][i] * hinv, a.p.p[2][i] * hinv};
-            const float vv[3] = {a.p.v[0][i], a.p.v[1][i], a.p.v[2][i]};
+            float f[3];
 #pragma unroll
-            for (int ax = 0; ax < 3; ax++) {
-                float cvec[3] = {0.f, 0.f, 0.f};
+            for (int d = 0; d < 3; d++) f[d] = a.p.p[d][i] * hinv - (float)cc[d];
+            float wt[3][3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) tent3(f[d], wt[d]);
+            if (role == 0) {
+                float cm[3] = {0.f, 0.f, 0.f};
                 if (APIC) {
-                    cvec[0] = a.p.c[3 * ax][i];
-                    cvec[1] = a.p.c[3 * ax + 1][i];
-                    cvec[2] = a.p.c[3 * ax + 2][i];
-                }
-                // stencil of MacGrid::getFacesAround (macGrid.cpp:142-181)
-                int b[3];
-                float d0[3];
 #pragma unroll
-                for (int dd = 0; dd < 3; dd++) {
-                    const float off = (dd == ax) ? 0.f : 0.5f;
-                    b[dd] = (int)(g[dd] - off) - (dd == ax ? 1 : 0);
-                    // node of cell t for this face axis: t + 1 along ax, t + 0.5 across
-                    d0[dd] = g[dd] - ((float)b[dd] + (dd == ax ? 1.f : 0.5f));
+                    for (int q = 0; q < 3; q++) cm[q] = a.p.c[q][i];
                 }
-                const float w0[3] = {1.f - fabsf(d0[0]), 1.f - fabsf(d0[1]), 1.f - fabsf(d0[2])};
-                const float w1[3] = {1.f - fabsf(d0[0] - 1.f), 1.f - fabsf(d0[1] - 1.f),
-                                     1.f - fabsf(d0[2] - 1.f)};
+                p2g_face_axis<APIC, 0, 0, 18>(f, wt, a.p.v[0][i], cm, h, acc);
 #pragma unroll
-                for (int o = 0; o < 8; o++) {
-                    const int ox = o >> 2, oy = (o >> 1) & 1, oz = o & 1;
-                    const int lx = b[0] + ox - x0, ly = b[1] + oy - y0, lz = b[2] + oz - z0;
-                    if (lx < 0 || ly < 0 || lz < 0 || lx >= TX || ly >= TY || lz >= TZ) continue;
-                    const float w = (ox ? w1[0] : w0[0]) * (oy ? w1[1] : w0[1]) * (oz ? w1[2] : w0[2]);
-                    float contrib = vv[ax];
-                    if (APIC) {
-                        // c[ax] . (face.pos - pos) with face.pos - pos = -(g - node) * h
-                        const float ddx = d0[0] - (float)ox, ddy = d0[1] - (float)oy, ddz = d0[2] - (float)oz;
-                        contrib -= (cvec[0] * ddx + cvec[1] * ddy + cvec[2] * ddz) * h;
+                for (int ox = 0; ox < 3; ox++)
+#pragma unroll
+                    for (int oy = 0; oy < 3; oy++) {
+                        const float wxy = wt[0][ox] * wt[1][oy];
+#pragma unroll
+                        for (int oz = 0; oz < 3; oz++) acc[36 + (ox * 3 + oy) * 3 + oz] += wxy * wt[2][oz];
                     }
-                    const int li = (lx * TY + ly) * TZ + lz;
-                    atomicAdd(&s_vw[ax * TCELLS + li], contrib * w);
-                    atomicAdd(&s_w[ax * TCELLS + li], w);
-                }
-            }
-            // cell-centre density (MacGrid::getCellsAround, macGrid.cpp:188-202)
-            {
-                int b[3];
-                float d0[3];
+            } else {
+                float cmy[3] = {0.f, 0.f, 0.f}, cmz[3] = {0.f, 0.f, 0.f};
+                if (APIC) {
 #pragma unroll
-                for (int dd = 0; dd < 3; dd++) {
-                    b[dd] = (int)(g[dd] - 0.5f);
-                    d0[dd] = g[dd] - ((float)b[dd] + 0.5f);
+                    for (int q = 0; q < 3; q++) {
+                        cmy[q] = a.p.c[3 + q][i];
+                        cmz[q] = a.p.c[6 + q][i];
+                    }
                 }
-#pragma unroll
-                for (int o = 0; o < 8; o++) {
-                    const int ox = o >> 2, oy = (o >> 1) & 1, oz = o & 1;
-                    const int lx = b[0] + ox - x0, ly = b[1] + oy - y0, lz = b[2] + oz - z0;
-                    if (lx < 0 || ly < 0 || lz < 0 || lx >= TX || ly >= TY || lz >= TZ) continue;
-                    const float w = (1.f - fabsf(d0[0] - ox)) * (1.f - fabsf(d0[1] - oy)) *
-                                    (1.f - fabsf(d0[2] - oz));
-                    atomicAdd(&s_avg[(lx * TY + ly) * TZ + lz], w);
-                }
+                p2g_face_axis<APIC, 1, 0, 18>(f, wt, a.p.v[1][i], cmy, h, acc);
+                p2g_face_axis<APIC, 2, 36, 54>(f, wt, a.p.v[2][i], cmz, h, acc);
             }
+        }
+        if (role == 0) {
+            p2g_flush_axis<0, 0, 18>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
+#pragma unroll
+            for (int e = 0; e < 27; e++) {
+                if (acc[36 + e] == 0.f) continue;
+                const int lx = cx + e / 9 - 1 - x0, ly = cy + (e / 3) % 3 - 1 - y0, lz = cz + e % 3 - 1 - z0;
+                if (lx < 0 || ly < 0 || lz < 0 || lx >= PX || ly >= PY || lz >= PZ) continue;
+                atomicAdd(&s_avg[(lx * PY + ly) * PZ + lz], acc[36 + e]);
+            }
+        } else {
+            p2g_flush_axis<1, 0, 18>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
+            p2g_flush_axis<2, 36, 54>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
         }
     }
     __syncthreads();
-    for (int lc = threadIdx.x; lc < TCELLS; lc += blockDim.x) {
-        const int lz = lc % TZ, ly = (lc / TZ) % TY, lx = lc / (TZ * TY);
+    for (int lc = threadIdx.x; lc < PCELLS; lc += blockDim.x) {
+        const int lz = lc % PZ, ly = (lc / PZ) % PY, lx = lc / (PZ * PY);
         const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
         if (x >= a.g.nx || y >= a.g.ny || z >= a.g.nz) continue;
         const long long cell = gidx(a.g, x, y, z);
 #pragma unroll
         for (int ax = 0; ax < 3; ax++) {
-            const float w = s_w[ax * TCELLS + lc];
-            a.u[ax][cell] = (w > 1e-6f) ? s_vw[ax * TCELLS + lc] / w : 0.f;
+            const float w = s_w[ax * PCELLS + lc];
+            a.u[ax][cell] = (w > 1e-6f) ? s_vw[ax * PCELLS + lc] / w : 0.f;
         }
         a.flags[cell] = (a.cstart[cell + 1] > a.cstart[cell]) ? C_WATER : C_AIR;
         a.avg[cell] = s_avg[lc];
@@ -344,21 +420,21 @@ void launch_p2g(fsim_ctx* ctx) {
     for (int k = 0; k < 3; k++) a.u[k] = ctx->u[k];
     a.flags = ctx->flags;
     a.avg = ctx->avg;
-    a.ntx = ceil_div(g.nx, TX);
-    a.nty = ceil_div(g.ny, TY);
-    a.ntz = ceil_div(g.nz, TZ);
+    a.ntx = ceil_div(g.nx, PX);
+    a.nty = ceil_div(g.ny, PY);
+    a.ntz = ceil_div(g.nz, PZ);
     const int nb = a.ntx * a.nty * a.ntz;
     ctx->launches += 1;
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
-        cudaFuncSetAttribute(k_p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
+        cudaFuncSetAttribute(k_p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM_V2);
+        cudaFuncSetAttribute(k_p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM_V2);
         attr_set = true;
     }
     if (ctx->prm.transfer == FSIM_APIC)
-        k_p2g<true><<<nb, P2G_THREADS, P2G_SMEM, ctx->stream>>>(a);
+        k_p2g<true><<<nb, P2G_THREADS_V2, P2G_SMEM_V2, ctx->stream>>>(a);
     else
-        k_p2g<false><<<nb, P2G_THREADS, P2G_SMEM, ctx->stream>>>(a);
+        k_p2g<false><<<nb, P2G_THREADS_V2, P2G_SMEM_V2, ctx->stream>>>(a);
 }
 
 // P2G on caller-provided buffers (used by the allocation-free entry point in
@@ -373,16 +449,16 @@ void launch_p2g_raw(ParticleBuf p, const uint32_t* perm, const int* cstart, cons
     for (int k = 0; k < 3; k++) a.u[k] = u[k];
     a.flags = flags;
     a.avg = avg;
-    a.ntx = ceil_div(g.nx, TX);
-    a.nty = ceil_div(g.ny, TY);
-    a.ntz = ceil_div(g.nz, TZ);
+    a.ntx = ceil_div(g.nx, PX);
+    a.nty = ceil_div(g.ny, PY);
+    a.ntz = ceil_div(g.nz, PZ);
     const int nb = a.ntx * a.nty * a.ntz;
-    cudaFuncSetAttribute(k_p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
-    cudaFuncSetAttribute(k_p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
+    cudaFuncSetAttribute(k_p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM_V2);
+    cudaFuncSetAttribute(k_p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM_V2);
     if (apic)
-        k_p2g<true><<<nb, P2G_THREADS, P2G_SMEM, stream>>>(a);
+        k_p2g<true><<<nb, P2G_THREADS_V2, P2G_SMEM_V2, stream>>>(a);
     else
-        k_p2g<false><<<nb, P2G_THREADS, P2G_SMEM, stream>>>(a);
+        k_p2g<false><<<nb, P2G_THREADS_V2, P2G_SMEM_V2, stream>>>(a);
 }
 
 // TMA descriptors of the six face arrays (v2 x/y/z, v x/y/z): 3D tensors

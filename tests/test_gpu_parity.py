@@ -208,3 +208,48 @@ def test_sink_despawn_counts(gpu, port_lib):
     gp, _, _ = g.particles()
     op, _, _ = o.particles()
     assert np.abs(gp.astype(np.float64) - op).max() <= 2e-7
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_gfx_publish_matches_particles_and_density(gpu, pinned):
+    """ParticleGfxData (simulationManager.cpp:218-231): position, |v| and the
+    trilinear interpolation of avgPNum at the particle, in device order."""
+    import ctypes as C
+
+    grid = GridSpec(32)
+    pos = dam_break(grid, seed=2)
+    sim = N.Simulation(32, N.default_params(transfer=N.FLIP, resolution=32))
+    sim.set_particles(pos)
+    sim.step(DT32)
+    sim.step(DT32)
+    n = sim.n
+    arr = (N.ParticleGfx * n)()
+    rt = None
+    if pinned:
+        for name in ("libcudart.so.13", "libcudart.so"):
+            try:
+                rt = C.CDLL(name)
+                break
+            except OSError:
+                pass
+        assert rt.cudaHostRegister(C.cast(arr, C.c_void_p), C.c_size_t(C.sizeof(arr)), 0) == 0
+    got = C.c_int64()
+    assert sim.lib.fsim_fill_gfx(sim.ctx, arr, n, C.byref(got), N.HOST) == 0
+    if rt is not None:
+        rt.cudaHostUnregister(C.cast(arr, C.c_void_p))
+    gfx = np.frombuffer(arr, dtype=np.float32).reshape(n, 5)
+    p, v, _ = sim.particles()
+    avg = sim.grid(N.F_AVGPNUM).astype(np.float64)
+    assert np.array_equal(gfx[:, :3], p)
+    assert np.allclose(gfx[:, 3], np.linalg.norm(v.astype(np.float64), axis=1), rtol=1e-5, atol=1e-6)
+    g = p.astype(np.float64) * 32 - 0.5
+    b = np.floor(g).astype(int)
+    dens = np.zeros(n)
+    for ox in (0, 1):
+        for oy in (0, 1):
+            for oz in (0, 1):
+                x, y, z = b[:, 0] + ox, b[:, 1] + oy, b[:, 2] + oz
+                w = (1 - np.abs(g[:, 0] - x)) * (1 - np.abs(g[:, 1] - y)) * (1 - np.abs(g[:, 2] - z))
+                dens += w * avg[x, y, z]
+    assert np.allclose(gfx[:, 4], dens, rtol=1e-4, atol=1e-5)
+    sim.close()
