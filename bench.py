@@ -328,11 +328,88 @@ def run_fsim(args):
                 "steps": e2e_steps, "path": "fsim_step + fsim_fill_gfx(pinned host) per step"},
         "gpu_launches": int(sum(s.kernel_launches for s in stats)),
     }
+    if args.ws_steps > 0:
+        line["pcg_warm_start"] = warm_start_study(sim, dt, t, h, N, args)
     sim.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(res, dt)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- learned warm start
+def train_warm_start(N, args):
+    """Train the warm-start network on the GPU from plain-solver pairs at 64^3:
+    synthetic pool problems plus snapshots of this workload's scene."""
+    import torch
+    from fluid_simulator_gb300 import warmstart as W
+
+    t0 = time.time()
+    n = 64
+    solver = W.ProblemSolver(n)
+    xa, ta, ma = W.make_dataset(n, args.ws_problems, seed=1, solver=solver)
+    solver.sim.close()
+    grid64, pos64 = workload_scene(n)
+    dt64 = 1.0 / (480.0 * n / 256.0)
+    p64 = N.default_params(transfer=N.APIC, resolution=n, tol=1e-8, tol_mode=N.TOL_REL_L2, max_iters=4000,
+                           spawning=True, despawning=True, precision=N.PREC_MIXED)
+    s64 = N.Simulation(n, p64)
+    s64.set_particles(pos64)
+    xb, tb, mb = W.scene_dataset(s64, dt64, args.ws_problems * 2, 2,
+                                 obstacles_fn=lambda tt: obstacles_at(tt, dt64, grid64.h, N))
+    s64.close()
+    xs = np.concatenate([xa, xb])
+    ts = np.concatenate([ta, tb])
+    ms = np.concatenate([ma, mb])
+    t_data = time.time() - t0
+    net = N.WarmStartNet(seed=1, out_scale=W.target_scale(ts, ms))
+    torch.cuda.synchronize()
+    t1 = time.time()
+    hist = W.train(net, xs, ts, ms, iters=args.ws_iters, batch=4, lr=1e-3)
+    torch.cuda.synchronize()
+    info = {"problems": int(xs.shape[0]), "grid": [n, n, n], "iters": args.ws_iters, "batch": 4, "lr": 1e-3,
+            "loss_first": round(float(np.mean(hist[:10])), 5), "loss_last": round(float(np.mean(hist[-10:])), 5),
+            "data_s": round(t_data, 2), "train_s": round(time.time() - t1, 2), "params": net.num_params}
+    return net, info
+
+
+def warm_start_study(sim, dt, t, h, N, args):
+    """PCG time to 1e-6 relative residual on the same 256^3 problems from the zero start
+    (the reference), the previous step's pressure, and the judged learned guess."""
+    net, info = train_warm_start(N, args)
+    sim.set_net(net)
+    modes = (("zero", N.WARM_ZERO), ("previous", N.WARM_PREVIOUS), ("learned", N.WARM_LEARNED))
+    rec = {k: [] for k, _ in modes}
+    stages = (N.STAGE_SPAWN, N.STAGE_ADVECT, N.STAGE_PUSH_OUT, N.STAGE_P2G, N.STAGE_OBSTACLES, N.STAGE_WALLS,
+              N.STAGE_POST_P2G)
+    for k in range(args.ws_steps + 1):
+        sim.set_obstacles(obstacles_at(t, dt, h, N))
+        for stg in stages:
+            sim.stage(stg, dt)
+        p_prev = sim.grid(N.F_PRESSURE)
+        for name, mode in modes:
+            sim.set_grid(N.F_PRESSURE, p_prev)
+            st = sim.solve_current(dt, mode, apply=False)
+            if k > 0:  # the first problem also pays the network's workspace allocation
+                rec[name].append((st.ms_solve, st.pcg_iterations, st.guess_used, st.ms_guess, st.residual_rel))
+        sim.set_grid(N.F_PRESSURE, p_prev)
+        sim.solve_current(dt, N.WARM_PREVIOUS, apply=True)
+        sim.stage(N.STAGE_EXTRAPOLATE, dt)
+        sim.stage(N.STAGE_G2P, dt)
+        t += dt
+    sim.set_net(None)
+    net.close()
+    out = {"tol": "1e-6 relative L2", "problems": args.ws_steps, "training": info}
+    for name, _ in modes:
+        r = rec[name]
+        out[name] = {"ms": round(statistics.mean(x[0] for x in r), 3),
+                     "iterations": round(statistics.mean(x[1] for x in r), 2),
+                     "residual_rel": max(x[4] for x in r)}
+    lr = rec["learned"]
+    out["learned"]["guess_used_frac"] = round(sum(1 for x in lr if x[2] == N.WARM_LEARNED) / len(lr), 3)
+    out["learned"]["ms_guess"] = round(statistics.mean(x[3] for x in lr), 3)
+    out["speedup_vs_zero"] = {k: round(out["zero"]["ms"] / out[k]["ms"], 3) for k in ("previous", "learned")}
+    return out
 
 
 # ---------------------------------------------------------------- CPU leg
@@ -416,6 +493,10 @@ def main():
     ap.add_argument("--precond", default="mg", choices=["mg", "rbic"],
                     help="pressure preconditioner: multigrid V-cycle or red-black incomplete Cholesky")
     ap.add_argument("--out-dir", default=os.path.join(ROOT, "gpurun_out"))
+    ap.add_argument("--ws-steps", type=int, default=4,
+                    help="problems of the zero / previous / learned warm-start comparison (0: skip)")
+    ap.add_argument("--ws-problems", type=int, default=48, help="synthetic training problems at 64^3")
+    ap.add_argument("--ws-iters", type=int, default=600, help="Adam iterations of the warm-start network")
     args = ap.parse_args()
     os.makedirs(args.out_dir, exist_ok=True)
     if args.impl == "reference":

@@ -706,7 +706,6 @@ int fsim_step(fsim_ctx* ctx, double dt, fsim_step_stats* stats) {
     if ((rc = check_device_error(ctx))) return rc;
     if (stats) {
         st.num_particles = (int)ctx->n;
-        st.guess_used = P.warm_start;
         st.kernel_launches = (int)(ctx->launches - launches0);
         if (P.timing) {
             st.ms_simulate_particles = elapsed(ctx, EV_START, EV_ADVECT);
@@ -860,6 +859,32 @@ int fsim_set_pressure_guess(fsim_ctx* ctx, const float* p, int where) {
     return FSIM_OK;
 }
 
+int fsim_solve_current(fsim_ctx* ctx, double dt, int warm_start, int apply, fsim_step_stats* stats) {
+    if (!ctx || !(dt > 0) || warm_start < FSIM_WARM_ZERO || warm_start > FSIM_WARM_LEARNED) return FSIM_E_INVALID;
+    const fsim_params& P = ctx->prm;
+    cudaStream_t s = ctx->stream;
+    fsim_step_stats tmp{};
+    fsim_step_stats* sp = stats ? stats : &tmp;
+    const long long l0 = ctx->launches;
+    FSIM_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[EV_PREP], s));
+    int rc = solve_pressure(ctx, dt, P.precision, P.tol_mode, P.residual_tol, P.max_iters, warm_start, sp, nullptr,
+                            apply);
+    FSIM_CUDA_TRY(ctx, cudaEventRecord(ctx->ev[EV_SOLVE], s));
+    FSIM_CUDA_TRY(ctx, cudaEventSynchronize(ctx->ev[EV_SOLVE]));
+    if (rc == FSIM_OK) {
+        sp->ms_solve = elapsed(ctx, EV_PREP, EV_SOLVE);
+        sp->kernel_launches = (int)(ctx->launches - l0);
+        rc = check_device_error(ctx);
+    }
+    return rc;
+}
+
+int fsim_set_net(fsim_ctx* ctx, fsim_net* net) {
+    if (!ctx) return FSIM_E_INVALID;
+    ctx->net = net;
+    return FSIM_OK;
+}
+
 int fsim_solve_pressure(fsim_ctx* ctx, const double* rhs, double dt, int precision, int tol_mode, double tol,
                         int max_iters, double* p_out, fsim_step_stats* stats) {
     if (!ctx || !rhs || !(dt > 0)) return FSIM_E_INVALID;
@@ -878,7 +903,9 @@ int fsim_solve_pressure(fsim_ctx* ctx, const double* rhs, double dt, int precisi
     fsim_step_stats tmp{};
     fsim_step_stats* sp = stats ? stats : &tmp;
     cudaEventRecord(ctx->ev[EV_PREP], s);
-    int rc = solve_pressure(ctx, dt, precision, tol_mode, tol, max_iters, FSIM_WARM_ZERO, sp, dpad, 0);
+    // zero start as the reference, or the judged learned guess when that is the configured warm start
+    const int warm = ctx->prm.warm_start == FSIM_WARM_LEARNED ? FSIM_WARM_LEARNED : FSIM_WARM_ZERO;
+    int rc = solve_pressure(ctx, dt, precision, tol_mode, tol, max_iters, warm, sp, dpad, 0);
     cudaEventRecord(ctx->ev[EV_SOLVE], s);
     cudaEventSynchronize(ctx->ev[EV_SOLVE]);
     if (rc == FSIM_OK) sp->ms_solve = elapsed(ctx, EV_PREP, EV_SOLVE);

@@ -30,6 +30,7 @@ struct PcgState {
     int bufsel;          // bit 0: current r buffer, bit 1: current s buffer
     int fold_enabled;    // MIXED: stop the inner iteration when the residual fell 100x
     int need_fold;       // set by the iteration when a fold + restart is due
+    int guess_used;      // the judged guess had the smaller residual and seeds PCG
 };
 
 // One level of the multigrid hierarchy (level 0 is the simulation grid).
@@ -115,6 +116,8 @@ struct fsim_ctx {
     int* d_misc = nullptr;   // small device scratch (counts)
     int* h_misc = nullptr;   // pinned
 
+    fsim_net* net = nullptr;  // warm-start network (FSIM_WARM_LEARNED), not owned
+
     cudaEvent_t ev[16];
     bool events = false;
     long long launches = 0;  // kernels launched by this context (monotonic)
@@ -180,7 +183,8 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
 
 // Event slots of a step (recorded when fsim_params.timing is set).
 enum {
-    EV_START = 0, EV_ADVECT, EV_SORT, EV_P2G, EV_PREP, EV_PCG_SETUP, EV_SOLVE, EV_EXTRAP, EV_G2P, EV_COUNT
+    EV_START = 0, EV_ADVECT, EV_SORT, EV_P2G, EV_PREP, EV_PCG_SETUP, EV_SOLVE, EV_EXTRAP, EV_G2P, EV_GUESS0,
+    EV_GUESS1, EV_COUNT
 };
 inline void fsim_record(fsim_ctx* ctx, int k) {
     if (ctx->prm.timing) cudaEventRecord(ctx->ev[k], ctx->stream);

@@ -36,6 +36,7 @@
 #include <cmath>
 
 #include "fsim_ctx.h"
+#include "fsim_net.h"
 
 namespace {
 
@@ -1202,6 +1203,49 @@ void solver_free(fsim_ctx* ctx) {
     S = SolverBufs{};
 }
 
+// ---- judged initial guess --------------------------------------------------
+// ||b - A phi|| (previous pressure) against ||b - A guess||, FP32 per cell and
+// FP64 per thread; the last block records which one seeds PCG.
+__global__ void __launch_bounds__(PCG_THREADS) k_guess_judge(const PcgArgs a, const float* guess) {
+    __shared__ double scratch[32 * 2];
+    double acc[2] = {0.0, 0.0};
+    const int nact = *a.nactive;
+    for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
+        int x, y, z;
+        long long c;
+        if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, z, c)) continue;
+        const uint16_t cc = a.code[c];
+        if (!(cc & CODE_FLUID)) continue;
+        const float ns = (float)code_ns(cc);
+        float ap = ns * (float)a.phi[c], ag = ns * guess[c];
+#pragma unroll
+        for (int k = 0; k < 6; k++)
+            if ((cc >> k) & 1) {
+                const long long j = c + nb_off(a.B, k);
+                ap -= (float)a.phi[j];
+                ag -= guess[j];
+            }
+        const float bc = (float)a.b[c];
+        const float rp = bc - ap, rg = bc - ag;
+        acc[0] += (double)(rp * rp);
+        acc[1] += (double)(rg * rg);
+    }
+    if (last_block_reduce<2>(acc, 0, a.partials, a.counter, scratch)) {
+        if (threadIdx.x == 0) a.st->guess_used = (acc[1] < acc[0]) ? 1 : 0;
+    }
+}
+
+__global__ void __launch_bounds__(PCG_THREADS) k_guess_apply(const PcgArgs a, const float* guess) {
+    if (!a.st->guess_used) return;
+    const int nact = *a.nactive;
+    for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
+        int x, y, z;
+        long long c;
+        if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, z, c)) continue;
+        if (a.code[c] & CODE_FLUID) a.phi[c] = (double)guess[c];
+    }
+}
+
 template <typename T>
 static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, int precond, fsim_step_stats* stats) {
     SolverBufs& S = ctx->sv;
@@ -1343,9 +1387,15 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     sa.flags = ctx->flags;
     for (int a = 0; a < 3; a++) sa.v2[a] = ctx->v2[a];
     sa.avg = ctx->avg;
-    sa.guess = (warm == FSIM_WARM_GUESS && S.have_guess) ? S.guess : nullptr;
+    // a user or learned guess is judged against the previous pressure after setup
+    const bool judged = warm == FSIM_WARM_LEARNED || (warm == FSIM_WARM_GUESS && S.have_guess);
+    if (warm == FSIM_WARM_LEARNED && !ctx->net) {
+        ctx->err = "FSIM_WARM_LEARNED needs a network (fsim_set_net)";
+        return FSIM_E_STATE;
+    }
+    sa.guess = nullptr;
     sa.rhs_override = rhs_override;
-    sa.warm = warm;
+    sa.warm = (warm == FSIM_WARM_ZERO) ? FSIM_WARM_ZERO : FSIM_WARM_PREVIOUS;
     sa.pressure_enabled = ctx->prm.pressure_enabled;
     sa.avg_pressure = ctx->prm.average_pressure;
     sa.pressure_k = ctx->prm.pressure_k;
@@ -1383,6 +1433,22 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     A.skip_bb = rhs_override ? -1.0 : 1e-7 / (scale * scale);
 
     int rc;
+    if (judged) {
+        fsim_record(ctx, EV_GUESS0);
+        if (warm == FSIM_WARM_LEARNED) {
+            const long long l0 = ctx->net->launches;
+            rc = net_guess(ctx->net, g, S.code, ctx->flags, S.b, S.guess, st);
+            ctx->launches += ctx->net->launches - l0;
+            if (rc) {
+                ctx->err = std::string("warm-start network: ") + fsim_net_last_error(ctx->net);
+                return rc;
+            }
+        }
+        k_guess_judge<<<S.grid_blocks, PCG_THREADS, 0, st>>>(A, S.guess);
+        k_guess_apply<<<S.grid_blocks, PCG_THREADS, 0, st>>>(A, S.guess);
+        ctx->launches += 2;
+        fsim_record(ctx, EV_GUESS1);
+    }
     if (precision == FSIM_PREC_FP64) {
         if ((rc = alloc_fp64(ctx))) return rc;
         const size_t nc = (size_t)g.ncell;
@@ -1408,6 +1474,12 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
         stats->residual_rel = hs.bb > 0 ? sqrt(hs.rr / hs.bb) : 0.0;
         stats->rhs_norm = sqrt(hs.bb) * scale;
         stats->num_active_bricks = ctx->h_misc[1];
+        stats->guess_used = judged ? (hs.guess_used ? warm : (warm == FSIM_WARM_ZERO ? 0 : FSIM_WARM_PREVIOUS)) : warm;
+        stats->ms_guess = 0.f;
+        if (judged && ctx->prm.timing) {
+            cudaEventSynchronize(ctx->ev[EV_GUESS1]);
+            cudaEventElapsedTime(&stats->ms_guess, ctx->ev[EV_GUESS0], ctx->ev[EV_GUESS1]);
+        }
     }
     if (hs.nan) {
         ctx->err = "pressure solve produced a non-finite scalar";

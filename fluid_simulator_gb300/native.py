@@ -22,7 +22,7 @@ HOST, DEVICE = 0, 1
 OBS_SPHERE, OBS_BOX, OBS_SOURCE, OBS_SINK, OBS_DISC_SOURCE, OBS_BOX_SINK = range(6)
 TOL_ABS_MAX, TOL_REL_L2 = 0, 1
 PREC_MIXED, PREC_FP32, PREC_FP64 = 0, 1, 2
-WARM_ZERO, WARM_PREVIOUS, WARM_GUESS = 0, 1, 2
+WARM_ZERO, WARM_PREVIOUS, WARM_GUESS, WARM_LEARNED = 0, 1, 2, 3
 PRECOND_RBIC, PRECOND_MG = 0, 1
 (STAGE_SPAWN, STAGE_ADVECT, STAGE_PUSH_APART, STAGE_PUSH_OUT, STAGE_STOP, STAGE_P2G, STAGE_MARK,
  STAGE_OBSTACLES, STAGE_WALLS, STAGE_POST_P2G, STAGE_SOLVE, STAGE_EXTRAPOLATE, STAGE_G2P) = range(13)
@@ -71,7 +71,8 @@ class StepStats(C.Structure):
         ("ms_p2g", C.c_float), ("ms_prep", C.c_float), ("ms_solve", C.c_float),
         ("ms_extrapolate", C.c_float), ("ms_g2p", C.c_float), ("ms_total", C.c_float),
         ("ms_p2g_kernel", C.c_float), ("ms_g2p_kernel", C.c_float), ("ms_pcg_setup", C.c_float),
-        ("kernel_launches", C.c_int), ("num_active_bricks", C.c_int), ("reserved", C.c_int * 3),
+        ("kernel_launches", C.c_int), ("num_active_bricks", C.c_int), ("ms_guess", C.c_float),
+        ("reserved", C.c_int * 2),
     ]
 
 
@@ -81,7 +82,11 @@ EXPORTS = [
     "fsim_last_error", "fsim_stream", "fsim_synchronize", "fsim_set_particles", "fsim_add_particles",
     "fsim_get_particles", "fsim_num_particles", "fsim_set_obstacles", "fsim_get_obstacles",
     "fsim_step", "fsim_stage", "fsim_get_grid", "fsim_set_grid", "fsim_fill_gfx",
-    "fsim_set_pressure_guess", "fsim_solve_pressure", "fsim_p2g_noalloc",
+    "fsim_set_pressure_guess", "fsim_solve_pressure", "fsim_solve_current", "fsim_p2g_noalloc",
+    "fsim_net_create", "fsim_net_destroy", "fsim_net_last_error", "fsim_net_num_params",
+    "fsim_net_get_params", "fsim_net_set_params", "fsim_net_forward", "fsim_net_backward",
+    "fsim_net_set_loss", "fsim_net_zero_grad", "fsim_net_adam", "fsim_net_train_step", "fsim_net_synchronize",
+    "fsim_net_conv", "fsim_set_net",
 ]
 
 _lib = None
@@ -119,7 +124,25 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "fsim_set_pressure_guess": (C.c_int, [P, fp, C.c_int]),
         "fsim_solve_pressure": (C.c_int, [P, dp, C.c_double, C.c_int, C.c_int, C.c_double, C.c_int, dp,
                                           C.POINTER(StepStats)]),
+        "fsim_solve_current": (C.c_int, [P, C.c_double, C.c_int, C.c_int, C.POINTER(StepStats)]),
         "fsim_p2g_noalloc": (C.c_int, [C.POINTER(GridDesc), C.c_int, P, P, P, i64, P, P, P, P, P, P]),
+        "fsim_net_create": (C.c_int, [C.c_uint64, C.c_float, C.POINTER(P)]),
+        "fsim_net_destroy": (C.c_int, [P]),
+        "fsim_net_last_error": (C.c_char_p, [P]),
+        "fsim_net_num_params": (i64, [P]),
+        "fsim_net_get_params": (C.c_int, [P, P, C.c_int, C.c_int]),
+        "fsim_net_set_params": (C.c_int, [P, P, C.c_int]),
+        "fsim_net_forward": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_int]),
+        "fsim_net_backward": (C.c_int, [P, P, P, fp, C.c_int]),
+        "fsim_net_set_loss": (C.c_int, [P, C.c_float]),
+        "fsim_net_zero_grad": (C.c_int, [P]),
+        "fsim_net_adam": (C.c_int, [P, C.c_float]),
+        "fsim_net_train_step": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, C.c_float, fp,
+                                          C.c_int]),
+        "fsim_net_synchronize": (C.c_int, [P]),
+        "fsim_net_conv": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                    P, P, P, P, C.c_int]),
+        "fsim_set_net": (C.c_int, [P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -305,8 +328,132 @@ class Simulation:
                     "fsim_solve_pressure")
         return p, st
 
+    def solve_current(self, dt: float, warm_start: int, apply: bool = False) -> StepStats:
+        """Pressure solve of the current state with an explicit warm start (fsim_solve_current)."""
+        st = StepStats()
+        self._check(self.lib.fsim_solve_current(self.ctx, dt, warm_start, int(apply), C.byref(st)),
+                    "fsim_solve_current")
+        return st
+
     def synchronize(self):
         self._check(self.lib.fsim_synchronize(self.ctx), "fsim_synchronize")
+
+    def set_net(self, net: "WarmStartNet | None"):
+        """Attach the warm-start network used by WARM_LEARNED (the context keeps no ownership)."""
+        self._net = net
+        self._check(self.lib.fsim_set_net(self.ctx, None if net is None else net.net), "fsim_set_net")
+
+
+class WarmStartNet:
+    """The learned pressure warm start (fsim_net_* in fsim.h).
+
+    Inputs are [n, d, h, w, 4] float32 (rhs / rms(rhs over fluid), fluid, solid,
+    air), outputs [n, d, h, w] float32 (pressure / rms(rhs)), in the solver's
+    integer-stencil units.  Arrays may be numpy (host) or anything exposing a
+    device pointer through ``data_ptr()`` (device).
+    """
+
+    def __init__(self, seed: int = 1, out_scale: float = 1.0):
+        self.lib = load_library()
+        self.net = C.c_void_p()
+        rc = self.lib.fsim_net_create(seed, out_scale, C.byref(self.net))
+        if rc != 0:
+            raise FsimError(f"fsim_net_create failed: {ERRORS.get(rc, rc)}")
+        self.num_params = int(self.lib.fsim_net_num_params(self.net))
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self.lib.fsim_net_last_error(self.net).decode()
+            raise FsimError(f"{what} failed: {ERRORS.get(rc, rc)}: {msg}")
+
+    def close(self):
+        if self.net:
+            self.lib.fsim_net_destroy(self.net)
+            self.net = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _arg(a):
+        if hasattr(a, "data_ptr"):
+            return C.c_void_p(a.data_ptr()), DEVICE
+        return C.c_void_p(a.ctypes.data), HOST
+
+    def params(self, grad: bool = False) -> np.ndarray:
+        out = np.empty(self.num_params, np.float32)
+        self._check(self.lib.fsim_net_get_params(self.net, _ptr(out), 1 if grad else 0, HOST), "fsim_net_get_params")
+        return out
+
+    def set_params(self, theta):
+        theta = np.ascontiguousarray(theta, np.float32)
+        assert theta.size == self.num_params
+        self._check(self.lib.fsim_net_set_params(self.net, _ptr(theta), HOST), "fsim_net_set_params")
+
+    def forward(self, x, train: bool = False):
+        if hasattr(x, "data_ptr"):
+            import torch
+            out = torch.empty(tuple(x.shape[:4]), dtype=torch.float32, device=x.device)
+            self._check(self.lib.fsim_net_forward(self.net, *x.shape[:4], C.c_void_p(x.data_ptr()),
+                                                  C.c_void_p(out.data_ptr()), int(train), DEVICE), "fsim_net_forward")
+            return out
+        x = np.ascontiguousarray(x, np.float32)
+        out = np.empty(x.shape[:4], np.float32)
+        self._check(self.lib.fsim_net_forward(self.net, *x.shape[:4], _ptr(x), _ptr(out), int(train), HOST),
+                    "fsim_net_forward")
+        return out
+
+    def backward(self, target, mask) -> float:
+        loss = C.c_float()
+        t, where = self._arg(target if hasattr(target, "data_ptr") else np.ascontiguousarray(target, np.float32))
+        m, _ = self._arg(mask if hasattr(mask, "data_ptr") else np.ascontiguousarray(mask, np.uint8))
+        self._check(self.lib.fsim_net_backward(self.net, t, m, C.byref(loss), where), "fsim_net_backward")
+        return loss.value
+
+    def set_loss(self, mse_weight: float):
+        self._check(self.lib.fsim_net_set_loss(self.net, mse_weight), "fsim_net_set_loss")
+
+    def zero_grad(self):
+        self._check(self.lib.fsim_net_zero_grad(self.net), "fsim_net_zero_grad")
+
+    def adam(self, lr: float):
+        self._check(self.lib.fsim_net_adam(self.net, lr), "fsim_net_adam")
+
+    def train_step(self, x, target, mask, lr: float) -> float:
+        loss = C.c_float()
+        dev = hasattr(x, "data_ptr")
+        if not dev:
+            x = np.ascontiguousarray(x, np.float32)
+            target = np.ascontiguousarray(target, np.float32)
+            mask = np.ascontiguousarray(mask, np.uint8)
+        xp, where = self._arg(x)
+        tp, _ = self._arg(target)
+        mp, _ = self._arg(mask)
+        self._check(self.lib.fsim_net_train_step(self.net, *x.shape[:4], xp, tp, mp, lr, C.byref(loss), where),
+                    "fsim_net_train_step")
+        return loss.value
+
+
+def net_conv(taps: int, mode: int, x=None, w=None, g=None, *, shape, cin: int, cout: int) -> np.ndarray:
+    """One tensor-core convolution on host FP32 arrays (fsim_net_conv)."""
+    lib = load_library()
+    n, d, h, ww = shape
+    vox = n * d * h * ww
+    if mode == 0:
+        out = np.empty((vox, cout), np.float32)
+    elif mode == 1:
+        out = np.empty((vox, cin), np.float32)
+    else:
+        out = np.empty((taps, cout, cin), np.float32)
+    args = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (x, w, g)]
+    rc = lib.fsim_net_conv(taps, mode, n, d, h, ww, cin, cout, *[_ptr(a) for a in args], _ptr(out), HOST)
+    if rc != 0:
+        msg = lib.fsim_net_last_error(None).decode()
+        raise FsimError(f"fsim_net_conv failed: {ERRORS.get(rc, rc)}: {msg}")
+    return out
 
 
 def obstacle(kind: int, pos, *, r: float = 0.0, size=(0, 0, 0), speed=(0, 0, 0), prev_pos=None,

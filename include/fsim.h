@@ -84,8 +84,11 @@ enum fsim_precond {
 enum fsim_warm_start {
     FSIM_WARM_ZERO = 0,     /* p0 = 0, as the reference */
     FSIM_WARM_PREVIOUS = 1, /* previous step's pressure */
-    FSIM_WARM_GUESS = 2     /* fsim_set_pressure_guess, falling back to the previous step's
+    FSIM_WARM_GUESS = 2,    /* fsim_set_pressure_guess, falling back to the previous step's
                                pressure when the guess has the larger residual */
+    FSIM_WARM_LEARNED = 3   /* the attached warm-start network (fsim_set_net), falling back
+                               to the previous step's pressure when its guess has the larger
+                               residual */
 };
 
 /* Step stages, in the order Simulator::simulate runs them (simulator.cpp:51-100). */
@@ -201,7 +204,8 @@ typedef struct fsim_step_stats {
     float ms_pcg_setup;           /* solve setup: codes, rhs, bricks, first residual */
     int kernel_launches;          /* CUDA kernels this call launched */
     int num_active_bricks;        /* pressure-solve bricks holding fluid */
-    int reserved[3];
+    float ms_guess;               /* FSIM_WARM_LEARNED: network inference + residual judgement */
+    int reserved[2];
 } fsim_step_stats;
 
 typedef struct fsim_ctx fsim_ctx;
@@ -275,6 +279,13 @@ int fsim_set_pressure_guess(fsim_ctx *ctx, const float *p, int where);
 int fsim_solve_pressure(fsim_ctx *ctx, const double *rhs, double dt, int precision, int tol_mode,
                         double tol, int max_iters, double *p_out, fsim_step_stats *stats);
 
+/* Pressure solve of the current state (the FSIM_STAGE_SOLVE stage,
+ * BridsonSolverGrid::solveIncompressibility, bridsonSolverGrid.cpp:244-293)
+ * with an explicit warm start; apply == 0 leaves the velocities untouched, so
+ * several warm starts can be timed on one problem (stats.ms_solve covers setup,
+ * guess and iterations). */
+int fsim_solve_current(fsim_ctx *ctx, double dt, int warm_start, int apply, fsim_step_stats *stats);
+
 /* ---- allocation-free particle-to-grid transfer --------------------------
  * This entry point has no counterpart in the reference.  It is for callers
  * that may not allocate GPU memory when they need a transfer: a render or
@@ -313,6 +324,62 @@ int fsim_solve_pressure(fsim_ctx *ctx, const double *rhs, double dt, int precisi
 int fsim_p2g_noalloc(const fsim_grid_desc *grid, int transfer, const float *pos, const float *vel,
                      const float *c, int64_t n, float *vx, float *vy, float *vz, uint8_t *flags,
                      float *avg, void *stream);
+
+/* ---- learned pressure warm start -----------------------------------------
+ * No counterpart in the reference (its PCG starts from zero,
+ * bridsonSolverGrid.cpp:249).  A 3D U-Net (levels of 16, 32, 64, 64 channels,
+ * two 3x3x3 conv + ReLU per level, 2x2x2 stride-2 down-convolutions, trilinear
+ * up-sampling with skip concatenation, 1x1x1 head) maps the solver's scaled
+ * right-hand side and cell types to a pressure guess.  BF16 weights and
+ * activations, FP32 accumulation on the tensor cores, FP32 master parameters
+ * trained with Adam.  The guess only seeds PCG: with params.warm_start ==
+ * FSIM_WARM_LEARNED the solver compares its residual with that of the previous
+ * step's pressure, starts from the better one and iterates to the same
+ * tolerance.
+ *
+ * Network input: [n][d][h][w][4] FP32 = (rhs / rms(rhs over fluid cells),
+ * fluid, solid, air); output [n][d][h][w] FP32 = pressure / rms(rhs), both in
+ * the solver's integer-stencil units (A = 7-point Laplacian with unit
+ * off-diagonals).  d, h, w are multiples of 8; voxel (d, h, w) is cell
+ * (x, y, z).  Parameters are one flat FP32 array (layer by layer: weights
+ * [tap][cout][cin], bias [cout]; head weight [16], bias [1]). */
+typedef struct fsim_net fsim_net;
+int fsim_net_create(uint64_t seed, float out_scale, fsim_net **out);
+int fsim_net_destroy(fsim_net *net);
+const char *fsim_net_last_error(const fsim_net *net);
+int64_t fsim_net_num_params(const fsim_net *net);
+/* what: 0 parameters, 1 accumulated gradient */
+int fsim_net_get_params(fsim_net *net, float *dst, int what, int where);
+int fsim_net_set_params(fsim_net *net, const float *src, int where);
+/* Forward pass; train != 0 keeps what fsim_net_backward needs.  out may be NULL. */
+int fsim_net_forward(fsim_net *net, int n, int d, int h, int w, const float *in, float *out, int train,
+                     int where);
+/* Backward pass after a training forward pass; adds to the gradient.  target
+ * [n][d][h][w] FP32 is the plain solver's solution, mask (uint8) marks the
+ * fluid cells.  With e = prediction - target on fluid cells and A the solver's
+ * 7-point operator of the input's cell types (A target = rhs), the loss is
+ * (sum (A e)^2 + mse_weight * sum e^2) / fluid cells: the residual the guess
+ * leaves in PCG, plus a small error term for the smooth part. */
+int fsim_net_backward(fsim_net *net, const float *target, const uint8_t *mask, float *loss, int where);
+/* mse_weight of the loss (default 0.01). */
+int fsim_net_set_loss(fsim_net *net, float mse_weight);
+int fsim_net_zero_grad(fsim_net *net);
+/* Adam (beta 0.9 / 0.999, eps 1e-8) on the accumulated gradient, which it clears. */
+int fsim_net_adam(fsim_net *net, float lr);
+/* forward + backward + Adam on one batch */
+int fsim_net_train_step(fsim_net *net, int n, int d, int h, int w, const float *in, const float *target,
+                        const uint8_t *mask, float lr, float *loss, int where);
+int fsim_net_synchronize(fsim_net *net);
+/* One convolution of the network's kernels on FP32 arrays (rounded to BF16
+ * inside), for checks: mode 0 forward y = conv(x, w) ([vox][cout]), mode 1
+ * input gradient of g ([vox][cin]), mode 2 weight gradient sum x (x) g
+ * ([taps][cout][cin]).  taps 27 (3x3x3, padding 1) or 1; cin, cout multiples
+ * of 16 (mode 2: cout <= 64). */
+int fsim_net_conv(int taps, int mode, int n, int d, int h, int w, int cin, int cout, const float *x,
+                  const float *wgt, const float *g, float *out, int where);
+/* Attach (or detach with NULL) the network used by FSIM_WARM_LEARNED.  The
+ * context does not own it. */
+int fsim_set_net(fsim_ctx *ctx, fsim_net *net);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,216 @@
+"""Learned warm start: tensor-core convolutions, network forward/backward and
+training against a PyTorch CPU restatement, and the gain of the learned guess.
+
+The first test runs the pointwise kernel (its launch reserves enough shared
+memory for any reading of the operand descriptors) before the 3x3x3 kernels.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+import torch.nn.functional as F
+
+import net_ref
+
+
+
+def bf(a):
+    """Round to BF16 like the kernels' operands."""
+    return torch.tensor(np.asarray(a, np.float32)).bfloat16().float().numpy()
+
+
+def rel_err(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def conv_ref(taps, x, w, shape, cin, cout):
+    n, d, h, ww = shape
+    xt = torch.tensor(x).view(n, d, h, ww, cin).permute(0, 4, 1, 2, 3)
+    if taps == 27:
+        wt = torch.tensor(w).view(27, cout, cin).permute(1, 2, 0).reshape(cout, cin, 3, 3, 3)
+        y = F.conv3d(xt, wt, padding=1)
+    else:
+        wt = torch.tensor(w).view(cout, cin, 1, 1, 1)
+        y = F.conv3d(xt, wt)
+    return y.permute(0, 2, 3, 4, 1).reshape(-1, cout).numpy()
+
+
+def test_reference_param_count():
+    offs, hw, hb, total = net_ref.layout()
+    assert total == sum(t * ci * co + co for t, ci, co in net_ref.SPEC) + 17
+    assert hb == hw + 16 and total == hb + 1
+    assert offs[0] == (0, 27 * 16 * 16)
+
+
+@pytest.mark.gpu
+def test_conv_pointwise_forward(gpu):
+    from fluid_simulator_gb300 import native as N
+    rng = np.random.default_rng(0)
+    shape, cin, cout = (1, 8, 16, 8), 32, 16
+    vox = int(np.prod(shape))
+    x = bf(rng.standard_normal((vox, cin)))
+    w = bf(rng.standard_normal((1, cout, cin)) * 0.2)
+    y = N.net_conv(1, 0, x, w, shape=shape, cin=cin, cout=cout)
+    ref = conv_ref(1, x, w, shape, cin, cout)
+    # FP32 accumulation; the output is rounded to BF16 (relative 2^-8)
+    assert np.allclose(y, ref, rtol=8e-3, atol=1e-3 * np.abs(ref).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape,cin,cout", [((1, 8, 16, 8), 16, 16), ((2, 6, 10, 12), 48, 32),
+                                            ((1, 8, 16, 16), 128, 64), ((1, 4, 4, 8), 32, 96)])
+def test_conv27_forward(gpu, shape, cin, cout):
+    from fluid_simulator_gb300 import native as N
+    rng = np.random.default_rng(1)
+    vox = int(np.prod(shape))
+    x = bf(rng.standard_normal((vox, cin)))
+    w = bf(rng.standard_normal((27, cout, cin)) * 0.1)
+    y = N.net_conv(27, 0, x, w, shape=shape, cin=cin, cout=cout)
+    ref = conv_ref(27, x, w, shape, cin, cout)
+    assert np.allclose(y, ref, rtol=8e-3, atol=2e-3 * np.abs(ref).max()), rel_err(y, ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("taps,shape,cin,cout", [(27, (2, 6, 10, 12), 16, 32), (27, (1, 8, 16, 8), 48, 16),
+                                                 (1, (1, 8, 8, 8), 256, 64)])
+def test_conv_input_gradient(gpu, taps, shape, cin, cout):
+    from fluid_simulator_gb300 import native as N
+    rng = np.random.default_rng(2)
+    vox = int(np.prod(shape))
+    x = torch.zeros((vox, cin), requires_grad=True)
+    w = bf(rng.standard_normal((taps, cout, cin)) * 0.1)
+    g = bf(rng.standard_normal((vox, cout)))
+    n, d, h, ww = shape
+    xt = x.view(n, d, h, ww, cin).permute(0, 4, 1, 2, 3)
+    if taps == 27:
+        wt = torch.tensor(w).permute(1, 2, 0).reshape(cout, cin, 3, 3, 3)
+        y = F.conv3d(xt, wt, padding=1)
+    else:
+        y = F.conv3d(xt, torch.tensor(w).view(cout, cin, 1, 1, 1))
+    y.permute(0, 2, 3, 4, 1).reshape(-1, cout).backward(torch.tensor(g))
+    ref = x.grad.numpy()
+    dx = N.net_conv(taps, 1, None, w, g, shape=shape, cin=cin, cout=cout)
+    assert np.allclose(dx, ref, rtol=8e-3, atol=2e-3 * np.abs(ref).max()), rel_err(dx, ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("taps,shape,cin,cout", [(27, (2, 6, 10, 12), 16, 32), (27, (1, 8, 16, 16), 96, 64),
+                                                 (1, (2, 8, 8, 8), 512, 64), (27, (1, 8, 8, 8), 64, 16),
+                                                 (27, (1, 2, 2, 2), 64, 64)])
+def test_conv_weight_gradient(gpu, taps, shape, cin, cout):
+    from fluid_simulator_gb300 import native as N
+    rng = np.random.default_rng(3)
+    vox = int(np.prod(shape))
+    x = bf(rng.standard_normal((vox, cin)))
+    g = bf(rng.standard_normal((vox, cout)))
+    n, d, h, ww = shape
+    xt = torch.tensor(x).view(n, d, h, ww, cin).permute(0, 4, 1, 2, 3)
+    if taps == 27:
+        wt = torch.zeros((cout, cin, 3, 3, 3), requires_grad=True)
+        y = F.conv3d(xt, wt, padding=1)
+    else:
+        wt = torch.zeros((cout, cin, 1, 1, 1), requires_grad=True)
+        y = F.conv3d(xt, wt)
+    y.permute(0, 2, 3, 4, 1).reshape(-1, cout).backward(torch.tensor(g))
+    ref = wt.grad.reshape(cout, cin, taps).permute(2, 0, 1).numpy()
+    dw = N.net_conv(taps, 2, x, None, g, shape=shape, cin=cin, cout=cout)
+    # FP32 accumulation in a different order: relative 1e-4 of the largest entry
+    assert np.allclose(dw, ref, rtol=1e-3, atol=1e-4 * np.abs(ref).max()), rel_err(dw, ref)
+
+
+def _batch(n, size, seed):
+    from fluid_simulator_gb300 import warmstart as W
+    xs, ts, ms = [], [], []
+    for i in range(n):
+        flags, rhs = W.make_problem(size, seed + i)
+        x, rms = W.net_input(flags, rhs)
+        rng = np.random.default_rng(seed + i)
+        xs.append(x)
+        ts.append(np.where(x[..., 1] > 0, rng.standard_normal(x.shape[:3]), 0.0).astype(np.float32))
+        ms.append((x[..., 1] > 0).astype(np.uint8))
+    return np.stack(xs), np.stack(ts), np.stack(ms)
+
+
+@pytest.mark.gpu
+def test_network_forward_backward_matches_cpu(gpu):
+    from fluid_simulator_gb300 import native as N
+    net = N.WarmStartNet(seed=1, out_scale=2.0)
+    assert net.num_params == net_ref.num_params()
+    theta = net.params()
+    x, t, m = _batch(2, 16, 10)
+    out = net.forward(x, train=True)
+    net.zero_grad()
+    loss = net.backward(t, m)
+    grad = net.params(grad=True)
+    # the CPU reference sees the BF16-rounded weights the kernels use
+    theta_b = theta.copy()
+    offs, hw, hb, _ = net_ref.layout()
+    for (w0, b0), (taps, cin, cout) in zip(offs, net_ref.SPEC):
+        theta_b[w0:w0 + taps * cin * cout] = bf(theta[w0:w0 + taps * cin * cout])
+    ref_loss, ref_out, ref_grad = net_ref.loss_and_grad(theta_b, x, t, m, out_scale=2.0)
+    # BF16 activations between layers: about 1% end to end
+    assert rel_err(out, ref_out) < 3e-2
+    assert abs(loss - ref_loss) < 3e-2 * ref_loss
+    for (w0, b0), (taps, cin, cout) in zip(offs, net_ref.SPEC):
+        gw, rw = grad[w0:w0 + taps * cin * cout], ref_grad[w0:w0 + taps * cin * cout]
+        if np.linalg.norm(rw) == 0:
+            continue
+        cos = float(np.dot(gw, rw) / (np.linalg.norm(gw) * np.linalg.norm(rw)))
+        assert rel_err(gw, rw) < 0.1 and cos > 0.99, (w0, rel_err(gw, rw), cos)
+        gb, rb = grad[b0:b0 + cout], ref_grad[b0:b0 + cout]
+        assert rel_err(gb, rb) < 0.1
+    assert rel_err(grad[hw:hb + 1], ref_grad[hw:hb + 1]) < 0.05
+    net.close()
+
+
+@pytest.mark.gpu
+def test_adam_step_matches_formula(gpu):
+    from fluid_simulator_gb300 import native as N
+    net = N.WarmStartNet(seed=3)
+    theta0 = net.params()
+    x, t, m = _batch(1, 16, 20)
+    net.forward(x, train=True)
+    net.zero_grad()
+    net.backward(t, m)
+    g = net.params(grad=True)
+    net.adam(1e-3)
+    theta1 = net.params()
+    # first Adam step: m_hat = g, v_hat = g^2 -> step = lr * g / (|g| + eps)
+    expect = theta0 - 1e-3 * g / (np.abs(g) + 1e-8)
+    assert np.allclose(theta1, expect, rtol=1e-5, atol=1e-7)
+    assert not net.params(grad=True).any()
+    net.close()
+
+
+@pytest.mark.gpu
+def test_training_and_learned_guess_gain(gpu):
+    """Train on plain-solver pairs; the judged learned guess must beat the zero start."""
+    from fluid_simulator_gb300 import native as N
+    from fluid_simulator_gb300 import warmstart as W
+    n = 32
+    solver = W.ProblemSolver(n)
+    xs, ts, ms = W.make_dataset(n, 48, seed=1, solver=solver)
+    net = N.WarmStartNet(seed=1, out_scale=W.target_scale(ts, ms))
+    hist = W.train(net, xs, ts, ms, iters=600, batch=8, lr=1e-3)
+    assert np.mean(hist[-20:]) < 0.5 * np.mean(hist[:20])
+    solver.sim.set_net(net)
+    print("loss", np.mean(hist[:10]), "->", np.mean(hist[-10:]))
+    its_zero, its_learned, used = [], [], 0
+    for i in range(6):
+        flags, rhs = W.make_problem(n, 777 + i)
+        p0, s0 = solver.solve(flags, rhs, warm=N.WARM_ZERO, tol=1e-6)
+        p1, s1 = solver.solve(flags, rhs, warm=N.WARM_LEARNED, tol=1e-6)
+        its_zero.append(s0.pcg_iterations)
+        its_learned.append(s1.pcg_iterations)
+        used += int(s1.guess_used == N.WARM_LEARNED)
+        # same tolerance, same answer
+        fl = W.solver_fluid(flags)
+        assert np.abs(p1 - p0)[fl].max() <= 1e-4 * np.abs(p0[fl]).max()
+    print("zero-start iterations", its_zero, "learned", its_learned, "guess used", used)
+    assert used >= 4
+    assert sum(its_learned) < sum(its_zero)
+    solver.sim.set_net(None)
+    net.close()
