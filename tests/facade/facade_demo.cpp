@@ -1,0 +1,90 @@
+// Drives the GPU library through the reference-shaped C++ facade the way the
+// reference's SimulationManager does (simulationManager.cpp:10-29,170-245):
+// build a BridsonSolverGrid, a HashedParticles and a Simulator, set the
+// obstacles, call simulate(dt) K times, read the particles back through
+// getParticleAt.  Input / output: raw float32 arrays (pos n x 3).
+//
+//   facade_demo <resolution> <steps> <dt> <transfer 0|1|2> <in_pos.bin> <out.bin>
+//
+// out.bin: int64 n, then pos (n x 3), v (n x 3), c (n x 9) as float32, then
+// int32 PCG iterations of the last step.
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <vector>
+
+#include "fsim_facade.hpp"
+
+using namespace genericfsim;
+
+int main(int argc, char** argv) {
+    if (argc != 7) {
+        std::cerr << "usage: facade_demo res steps dt transfer in_pos.bin out.bin\n";
+        return 2;
+    }
+    const double res = std::atof(argv[1]);
+    const int steps = std::atoi(argv[2]);
+    const double dt = std::atof(argv[3]);
+    const int transfer = std::atoi(argv[4]);
+    std::ifstream in(argv[5], std::ios::binary | std::ios::ate);
+    const std::streamsize bytes = in.tellg();
+    in.seekg(0);
+    std::vector<float> pos((size_t)bytes / 4);
+    in.read(reinterpret_cast<char*>(pos.data()), bytes);
+    const size_t n = pos.size() / 3;
+    try {
+        auto grid = std::make_shared<macgrid::BridsonSolverGrid>(glm::dvec3(1, 1, 1), (float)res, false, 1.0);
+        grid->isTopOfContainerSolid = true;
+        grid->pressureEnabled = false;
+        grid->incompressibilityMaxIterationCount = 200;
+        grid->residualTolerance = 1e-6;
+        const double h = 1.0 / res;
+        auto parts = std::make_shared<particles::HashedParticles>(0, h / 4, grid->dimensions, grid->cellD, false, 0.0);
+        std::vector<particles::Particle> ps(n);
+        for (size_t i = 0; i < n; i++) {
+            ps[i].pos = glm::dvec3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+            ps[i].v = glm::dvec3(0, 0, 0);
+            ps[i].c[0] = ps[i].c[1] = ps[i].c[2] = glm::dvec3(0, 0, 0);
+        }
+        parts->addParticles(std::move(ps));
+        simulator::Simulator::SimulatorConfig cfg;
+        cfg.transferType = (simulator::Simulator::P2G2PType)transfer;
+        cfg.flipRatio = 0.95f;
+        cfg.gravity = -9.81f;
+        cfg.pushApartEnabled = false;
+        simulator::Simulator sim(cfg, parts, grid);
+        sim.obstacles.push_back(std::make_unique<obstacle::SphericalObstacle>(0.15, glm::dvec3(0.6, 0.3, 0.5)));
+        for (int s = 0; s < steps; s++) {
+            sim.obstacles[0]->setNewPos(glm::dvec3(0.6 + 0.01 * s, 0.3, 0.5));
+            sim.obstacles[0]->calculateSpeed(dt);
+            sim.simulate(dt);
+        }
+        const auto dur = sim.getStepDuration();
+        const int its = (int)dur.at("Incompressibility it count");
+        const int m = parts->getParticleNum();
+        std::vector<float> p3((size_t)m * 3), v3((size_t)m * 3), c9((size_t)m * 9);
+        for (int i = 0; i < m; i++) {
+            const particles::Particle& q = parts->getParticleAt(i);
+            for (int a = 0; a < 3; a++) {
+                p3[3 * i + a] = (float)q.pos[a];
+                v3[3 * i + a] = (float)q.v[a];
+                for (int b = 0; b < 3; b++) c9[9 * i + 3 * a + b] = (float)q.c[a][b];
+            }
+        }
+        // a cell read through the grid mirror, as SimulationManager::getCellAt does
+        const macgrid::MacGridCell& cell = grid->getCellAt(glm::dvec3(0.3, 0.1, 0.5));
+        std::ofstream out(argv[6], std::ios::binary);
+        const int64_t mm = m;
+        out.write(reinterpret_cast<const char*>(&mm), 8);
+        out.write(reinterpret_cast<const char*>(p3.data()), p3.size() * 4);
+        out.write(reinterpret_cast<const char*>(v3.data()), v3.size() * 4);
+        out.write(reinterpret_cast<const char*>(c9.data()), c9.size() * 4);
+        out.write(reinterpret_cast<const char*>(&its), 4);
+        std::cout << "particles " << m << " its " << its << " cell_type " << (int)cell.type << "\n";
+    } catch (const std::exception& e) {
+        std::cerr << "error: " << e.what() << "\n";
+        return 1;
+    }
+    return 0;
+}

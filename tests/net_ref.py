@@ -34,7 +34,20 @@ def num_params() -> int:
     return layout()[3]
 
 
-def forward(theta: torch.Tensor, x: torch.Tensor, out_scale: float = 1.0) -> torch.Tensor:
+class _RoundBF16(torch.autograd.Function):
+    """Round to BF16 where the kernels store a BF16 tensor: the value going
+    forward and the gradient coming back."""
+
+    @staticmethod
+    def forward(ctx, x):
+        return x.bfloat16().float()
+
+    @staticmethod
+    def backward(ctx, g):
+        return g.bfloat16().float()
+
+
+def forward(theta: torch.Tensor, x: torch.Tensor, out_scale: float = 1.0, bf16: bool = False) -> torch.Tensor:
     offs, hw, hb, total = layout()
     assert theta.numel() == total
 
@@ -44,22 +57,27 @@ def forward(theta: torch.Tensor, x: torch.Tensor, out_scale: float = 1.0) -> tor
         w = theta[w0:w0 + taps * cin * cout].view(taps, cout, cin)
         return w, theta[b0:b0 + cout]
 
+    rnd = _RoundBF16.apply if bf16 else (lambda t: t)
+
     def conv(l, inp):
         w, b = wb(l)
         wt = w.permute(1, 2, 0).reshape(w.shape[1], w.shape[2], 3, 3, 3)
-        return F.relu(F.conv3d(inp, wt, b, padding=1))
+        return rnd(F.relu(F.conv3d(inp, wt, b, padding=1)))
 
     def down(l, inp):
         w, b = wb(l)
         C = inp.shape[1]
         wt = w[0].view(w.shape[1], 8, C).permute(0, 2, 1).reshape(w.shape[1], C, 2, 2, 2)
-        return F.relu(F.conv3d(inp, wt, b, stride=2))
+        return rnd(F.relu(F.conv3d(rnd(inp), wt, b, stride=2)))
 
     def up(t):
-        return F.interpolate(t, scale_factor=2, mode="trilinear", align_corners=False)
+        return rnd(F.interpolate(t, scale_factor=2, mode="trilinear", align_corners=False))
+
+    def cat(a, b):
+        return rnd(torch.cat([a, b], 1))
 
     x0 = x.permute(0, 4, 1, 2, 3)
-    x0 = torch.cat([x0, torch.zeros(x0.shape[0], 12, *x0.shape[2:], dtype=x0.dtype)], 1)
+    x0 = rnd(torch.cat([x0, torch.zeros(x0.shape[0], 12, *x0.shape[2:], dtype=x0.dtype)], 1))
     a0 = conv(0, x0)
     e0 = conv(1, a0)
     x1 = down(2, e0)
@@ -71,11 +89,11 @@ def forward(theta: torch.Tensor, x: torch.Tensor, out_scale: float = 1.0) -> tor
     x3 = down(8, e2)
     a3 = conv(9, x3)
     b3 = conv(10, a3)
-    c2 = conv(11, torch.cat([up(b3), e2], 1))
+    c2 = conv(11, cat(up(b3), e2))
     d2 = conv(12, c2)
-    c1 = conv(13, torch.cat([up(d2), e1], 1))
+    c1 = conv(13, cat(up(d2), e1))
     d1 = conv(14, c1)
-    c0 = conv(15, torch.cat([up(d1), e0], 1))
+    c0 = conv(15, cat(up(d1), e0))
     d0 = conv(16, c0)
     out = torch.einsum("ncdhw,c->ndhw", d0, theta[hw:hw + 16]) + theta[hb]
     return out_scale * out
@@ -96,12 +114,12 @@ def operator(e: torch.Tensor, m: torch.Tensor, solid: torch.Tensor) -> torch.Ten
     return m * (ns * e - nb)
 
 
-def loss_and_grad(theta_np, x_np, t_np, m_np, out_scale: float = 1.0, mse_weight: float = 0.01):
+def loss_and_grad(theta_np, x_np, t_np, m_np, out_scale: float = 1.0, mse_weight: float = 0.01, bf16: bool = True):
     theta = torch.tensor(theta_np, dtype=torch.float32, requires_grad=True)
     x = torch.tensor(x_np, dtype=torch.float32)
     t = torch.tensor(t_np, dtype=torch.float32)
     m = torch.tensor(m_np.astype("float32"))
-    out = forward(theta, x, out_scale)
+    out = forward(theta, x, out_scale, bf16=bf16)
     e = (out - t) * m
     r = operator(e, m, x[..., 2])
     loss = ((r * r).sum() + mse_weight * (e * e).sum()) / m.sum().clamp(min=1)

@@ -150,18 +150,20 @@ def test_network_forward_backward_matches_cpu(gpu):
     offs, hw, hb, _ = net_ref.layout()
     for (w0, b0), (taps, cin, cout) in zip(offs, net_ref.SPEC):
         theta_b[w0:w0 + taps * cin * cout] = bf(theta[w0:w0 + taps * cin * cout])
+    # the reference rounds to BF16 wherever the kernels store BF16 (activations
+    # going forward, their gradients coming back); what remains is FP32
+    # summation order and the rounding flips it causes
     ref_loss, ref_out, ref_grad = net_ref.loss_and_grad(theta_b, x, t, m, out_scale=2.0)
-    # BF16 activations between layers: about 1% end to end
-    assert rel_err(out, ref_out) < 3e-2
-    assert abs(loss - ref_loss) < 3e-2 * ref_loss
+    assert rel_err(out, ref_out) < 1e-2
+    assert abs(loss - ref_loss) < 2e-2 * ref_loss
     for (w0, b0), (taps, cin, cout) in zip(offs, net_ref.SPEC):
         gw, rw = grad[w0:w0 + taps * cin * cout], ref_grad[w0:w0 + taps * cin * cout]
         if np.linalg.norm(rw) == 0:
             continue
         cos = float(np.dot(gw, rw) / (np.linalg.norm(gw) * np.linalg.norm(rw)))
-        assert rel_err(gw, rw) < 0.1 and cos > 0.99, (w0, rel_err(gw, rw), cos)
+        assert rel_err(gw, rw) < 0.05 and cos > 0.998, (w0, rel_err(gw, rw), cos)
         gb, rb = grad[b0:b0 + cout], ref_grad[b0:b0 + cout]
-        assert rel_err(gb, rb) < 0.1
+        assert rel_err(gb, rb) < 0.05
     assert rel_err(grad[hw:hb + 1], ref_grad[hw:hb + 1]) < 0.05
     net.close()
 
