@@ -168,6 +168,10 @@ BYTES_G2P_PER_PARTICLE = {0: 24, 1: 36, 2: 60}
 BYTES_G2P_PER_CELL = {0: 12, 1: 24, 2: 12}
 BYTES_GRID_PER_CELL = 150
 BYTES_PCG_PER_FLUID_CELL_ITER = 60
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one k_p2g / k_g2p launch per
+# particle, from full ncu captures of the same scene at 128^3 (8.0M particles; cells per particle
+# are the same at 256^3, so the per-particle figure scales to the 256^3 launch)
+DRAM_BYTES_PER_PARTICLE = {"p2g": 639.665e6 / 7999554, "g2p": None}
 
 
 def dist_setup(n_gpus: int):
@@ -211,7 +215,8 @@ def run_fsim(args):
     precond = {"mg": N.PRECOND_MG, "rbic": N.PRECOND_RBIC}[args.precond]
     p = N.default_params(transfer=N.APIC, resolution=res, tol=1e-6, tol_mode=N.TOL_REL_L2, max_iters=2000,
                          spawning=True, despawning=True, timing=True, precision=N.PREC_MIXED,
-                         warm_start=N.WARM_ZERO, precond=precond)
+                         warm_start=N.WARM_ZERO, precond=precond, mg_sweeps=args.mg_sweeps,
+                         mg_coarse_sweeps=args.mg_coarse_sweeps)
     sim = N.Simulation(res, p)
     sim.set_particles(pos)
     del pos
@@ -318,7 +323,11 @@ def run_fsim(args):
         "step_roofline": {"bytes": step_bytes, "achieved_gbs": round(step_bytes / (ms_step / 1e3) / 1e9, 1),
                           "frac": round(step_bytes / (ms_step / 1e3) / 1e9 / peak, 4)},
         "roofline": {"kernel": f"k_{dominant}", "bound": "hbm", "achieved": round(dk["gbs"], 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(dk["frac"], 4), "traffic": None,
+                     "unit": "GB/s", "frac": round(dk["frac"], 4),
+                     "traffic": (round(DRAM_BYTES_PER_PARTICLE[dominant] * np_mean)
+                                 if DRAM_BYTES_PER_PARTICLE[dominant] else None),
+                     "traffic_source": "ncu capture at 128^3 scaled per particle",
+                     "algorithmic_bytes": round(dk["bytes"]),
                      "peak_source": peak_kind,
                      "all": {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
                              for k, v in kernels.items()}},
@@ -493,6 +502,10 @@ def main():
     ap.add_argument("--precond", default="mg", choices=["mg", "rbic"],
                     help="pressure preconditioner: multigrid V-cycle or red-black incomplete Cholesky")
     ap.add_argument("--out-dir", default=os.path.join(ROOT, "gpurun_out"))
+    ap.add_argument("--mg-sweeps", type=int, default=0,
+                    help="multigrid smoothing sweeps before and after the coarse correction (0: library default)")
+    ap.add_argument("--mg-coarse-sweeps", type=int, default=0,
+                    help="multigrid sweeps on the coarser levels (0: as --mg-sweeps)")
     ap.add_argument("--ws-steps", type=int, default=4,
                     help="problems of the zero / previous / learned warm-start comparison (0: skip)")
     ap.add_argument("--ws-problems", type=int, default=48, help="synthetic training problems at 64^3")

@@ -66,6 +66,7 @@ struct SolverBufs {
     int grid_blocks = 0;          // persistent grid size for brick kernels
     double last_scale = 1.0;      // dt / (rho h^2) of the last solve
     std::vector<MGLevelBufs> mg;  // multigrid hierarchy (built at allocation)
+    int mg_cluster = 0;           // CTAs in the coarse-V-cycle cluster (0: separate launches)
     cudaGraphExec_t iter_exec = nullptr;  // one PCG iteration, captured on first use
     int iter_key = -1;                    // configuration the graph was captured for
     int iter_kernels = 0;                 // kernels in that graph

@@ -515,11 +515,12 @@ int launch_conv_mma(const ConvLaunch& L, cudaStream_t s) {
     a.err = L.err;
     const int a_bytes = taps == 27 ? Halo<27>::A_BYTES : Halo<1>::A_BYTES;
     const int stage = a_bytes + 2 * taps * a.nt * 16;
-    int stages = (SMEM_LIMIT - 256) / stage;
-    if (stages > 3) stages = 3;
+    if (stage + 128 > SMEM_LIMIT) return FSIM_E_INVALID;
+    // as many pipeline stages (<= 3, <= chunks) as keep two CTAs on an SM: the
+    // second CTA's loads and epilogue overlap the first one's MMAs
     const int nchunk = L.cin / 16;
-    if (stages > nchunk) stages = nchunk;
-    if (stages < 1) return FSIM_E_INVALID;
+    int stages = 1;
+    while (stages < 3 && stages < nchunk && (stages + 1) * stage + 128 <= SMEM_LIMIT / 2) stages++;
     a.stages = stages;
     int smem = stages * stage + 128;
     // the pointwise kernel's accumulator can take all of TMEM: one CTA per SM

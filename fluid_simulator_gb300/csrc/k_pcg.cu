@@ -560,6 +560,19 @@ __device__ __forceinline__ float nbsum(const Q7& q, int i, uint16_t cc) {
     return s;
 }
 
+// all quads of a coarse level, thread i0 + k * step
+template <typename F>
+__device__ __forceinline__ void mg_for_range(const MGLev& L, long long i0, long long step, F&& fn) {
+    const int qz = L.pz >> 2;
+    const long long n = (long long)L.nx * L.ny * qz;
+    for (long long i = i0; i < n; i += step) {
+        const int z0 = (int)(i % qz) << 2;
+        const long long t = i / qz;
+        const int y = (int)(t % L.ny), x = (int)(t / L.ny);
+        fn(x, y, z0, ((long long)x * L.ny + y) * L.pz + z0);
+    }
+}
+
 template <bool FINE, typename F>
 __device__ __forceinline__ void mg_for_quads(const PcgArgs& A, const MGLev& L, F&& fn) {
     if (FINE) {
@@ -587,31 +600,34 @@ __device__ __forceinline__ void mg_for_quads(const PcgArgs& A, const MGLev& L, F
 
 __device__ __forceinline__ long long lev_sx(const MGLev& L) { return (long long)L.pz * L.ny; }
 
-// one red-black Gauss-Seidel half sweep; first: the other colour is still zero
+// one red-black Gauss-Seidel half sweep of a quad; first: the other colour is still zero
+__device__ __forceinline__ void smooth_quad(const MGLev& L, const float* rhs, int color, int first, int x, int y,
+                                            int z0, long long c0) {
+    uint16_t cc[4];
+    codes4(L.code, c0, cc);
+    if (!any_fluid(cc)) return;
+    float f[4];
+    unpack4(ld4(rhs + c0), f);
+    Q7 q;
+    if (first) unpack4(ld4(L.x + c0), q.c);
+    else load_q7(q, L.x, c0, L, x, y, z0);
+    const int par = (x + y + z0) & 1;
+    float out[4] = {q.c[0], q.c[1], q.c[2], q.c[3]};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        if (((par ^ i) & 1) != color || !(cc[i] & CODE_FLUID)) continue;
+        float sum = f[i];
+        if (!first) sum += nbsum(q, i, cc[i]);
+        out[i] = sum * c_rcp[code_ns(cc[i])];
+    }
+    st4(L.x + c0, out);
+}
+
 template <bool FINE>
 __global__ void __launch_bounds__(PCG_THREADS) k_mg_smooth(const PcgArgs A, MGLev L, int color, int first) {
     if (A.st->done) return;
     const float* rhs = mg_rhs(A, L);
-    mg_for_quads<FINE>(A, L, [&](int x, int y, int z0, long long c0) {
-        uint16_t cc[4];
-        codes4(L.code, c0, cc);
-        if (!any_fluid(cc)) return;
-        float f[4];
-        unpack4(ld4(rhs + c0), f);
-        Q7 q;
-        if (first) unpack4(ld4(L.x + c0), q.c);
-        else load_q7(q, L.x, c0, L, x, y, z0);
-        const int par = (x + y + z0) & 1;
-        float out[4] = {q.c[0], q.c[1], q.c[2], q.c[3]};
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            if (((par ^ i) & 1) != color || !(cc[i] & CODE_FLUID)) continue;
-            float sum = f[i];
-            if (!first) sum += nbsum(q, i, cc[i]);
-            out[i] = sum * c_rcp[code_ns(cc[i])];
-        }
-        st4(L.x + c0, out);
-    });
+    mg_for_quads<FINE>(A, L, [&](int x, int y, int z0, long long c0) { smooth_quad(L, rhs, color, first, x, y, z0, c0); });
 }
 
 // the last post-smoothing half sweep (red, level 0) fused with z.r (modes 0/1 as k_red)
@@ -660,40 +676,35 @@ __global__ void __launch_bounds__(PCG_THREADS) k_mg_smooth_dot(const PcgArgs A, 
     }
 }
 
+__device__ __forceinline__ void residual_quad(const MGLev& L, const float* rhs, int x, int y, int z0, long long c0) {
+    uint16_t cc[4];
+    codes4(L.code, c0, cc);
+    if (!any_fluid(cc)) return;
+    float f[4];
+    unpack4(ld4(rhs + c0), f);
+    Q7 q;
+    load_q7(q, L.x, c0, L, x, y, z0);
+    float out[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        out[i] = (cc[i] & CODE_FLUID) ? f[i] - ((float)code_ns(cc[i]) * q.c[i] - nbsum(q, i, cc[i])) : 0.f;
+    st4(L.r + c0, out);
+}
+
 template <bool FINE>
 __global__ void __launch_bounds__(PCG_THREADS) k_mg_residual(const PcgArgs A, MGLev L) {
     if (A.st->done) return;
     const float* rhs = mg_rhs(A, L);
-    mg_for_quads<FINE>(A, L, [&](int x, int y, int z0, long long c0) {
-        uint16_t cc[4];
-        codes4(L.code, c0, cc);
-        if (!any_fluid(cc)) return;
-        float f[4];
-        unpack4(ld4(rhs + c0), f);
-        Q7 q;
-        load_q7(q, L.x, c0, L, x, y, z0);
-        float out[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-            out[i] = (cc[i] & CODE_FLUID) ? f[i] - ((float)code_ns(cc[i]) * q.c[i] - nbsum(q, i, cc[i])) : 0.f;
-        st4(L.r + c0, out);
-    });
+    mg_for_quads<FINE>(A, L, [&](int x, int y, int z0, long long c0) { residual_quad(L, rhs, x, y, z0, c0); });
 }
 
 // coarse f = 0.5 * sum_fine P[f,C] r_f  (= 4 R r), per coarse quad:
 // fine z 2 z0 - 1 .. 2 z0 + 8 come from the four fine quads at 2 z0 - 4 .. 2 z0 + 8
-__global__ void __launch_bounds__(PCG_THREADS) k_mg_restrict(const PcgState* st, MGLev F, MGLev Cl) {
-    if (st->done) return;
-    const int qz = Cl.pz >> 2;
-    const long long n = (long long)Cl.nx * Cl.ny * qz;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int cz0 = (int)(i % qz) << 2;
-        const long long t = i / qz;
-        const int cy = (int)(t % Cl.ny), cx = (int)(t / Cl.ny);
-        const long long ci = ((long long)cx * Cl.ny + cy) * Cl.pz + cz0;
+__device__ __forceinline__ void restrict_quad(const MGLev& F, const MGLev& Cl, int cx, int cy, int cz0, long long ci) {
+    {
         uint16_t ccc[4];
         codes4(Cl.code, ci, ccc);
-        if (!any_fluid(ccc)) continue;
+        if (!any_fluid(ccc)) return;
         float sum[4] = {0.f, 0.f, 0.f, 0.f};
         const int fz0 = 2 * cz0 - 4;  // first fine z loaded (a multiple of 4)
         for (int dx = -1; dx <= 2; dx++) {
@@ -740,46 +751,54 @@ __global__ void __launch_bounds__(PCG_THREADS) k_mg_restrict(const PcgState* st,
     }
 }
 
+__global__ void __launch_bounds__(PCG_THREADS) k_mg_restrict(const PcgState* st, MGLev F, MGLev Cl) {
+    if (st->done) return;
+    mg_for_range(Cl, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x,
+                 [&](int x, int y, int z0, long long c0) { restrict_quad(F, Cl, x, y, z0, c0); });
+}
+
 // fine x += P x_coarse on fluid fine cells, per fine quad: the quad's coarse z
 // neighbours are z0/2 - 1 .. z0/2 + 2
+__device__ __forceinline__ void prolong_quad(const MGLev& F, const MGLev& Cl, int x, int y, int z0, long long c0) {
+    uint16_t cc[4];
+    codes4(F.code, c0, cc);
+    if (!any_fluid(cc)) return;
+    const int px = (x & 1) ? x >> 1 : (x >> 1) - 1;  // lower coarse neighbour per axis
+    const int py = (y & 1) ? y >> 1 : (y >> 1) - 1;
+    const float wlx = (x & 1) ? 0.75f : 0.25f, wly = (y & 1) ? 0.75f : 0.25f;
+    const int zc = (z0 >> 1) - 1;
+    float sum[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int o = 0; o < 4; o++) {
+        const int ox = o >> 1, oy = o & 1;
+        const int cx = px + ox, cy = py + oy;
+        if (cx < 0 || cy < 0 || cx >= Cl.nx || cy >= Cl.ny) continue;
+        const float wxy = (ox ? 1.f - wlx : wlx) * (oy ? 1.f - wly : wly);
+        const long long row = ((long long)cx * Cl.ny + cy) * Cl.pz;
+        float cv[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int z = zc + k;
+            cv[k] = (z >= 0 && z < Cl.nz && (Cl.code[row + z] & CODE_FLUID)) ? Cl.x[row + z] : 0.f;
+        }
+        // lanes: z0 (lower zc, w 1/4), z0+1 (zc+1, 3/4), z0+2 (zc+1, 1/4), z0+3 (zc+2, 3/4)
+        sum[0] += wxy * (0.25f * cv[0] + 0.75f * cv[1]);
+        sum[1] += wxy * (0.75f * cv[1] + 0.25f * cv[2]);
+        sum[2] += wxy * (0.25f * cv[1] + 0.75f * cv[2]);
+        sum[3] += wxy * (0.75f * cv[2] + 0.25f * cv[3]);
+    }
+    float xv[4];
+    unpack4(ld4(F.x + c0), xv);
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        if (cc[i] & CODE_FLUID) xv[i] += sum[i];
+    st4(F.x + c0, xv);
+}
+
 template <bool FINE>
 __global__ void __launch_bounds__(PCG_THREADS) k_mg_prolong(const PcgArgs A, MGLev F, MGLev Cl) {
     if (A.st->done) return;
-    mg_for_quads<FINE>(A, F, [&](int x, int y, int z0, long long c0) {
-        uint16_t cc[4];
-        codes4(F.code, c0, cc);
-        if (!any_fluid(cc)) return;
-        const int px = (x & 1) ? x >> 1 : (x >> 1) - 1;  // lower coarse neighbour per axis
-        const int py = (y & 1) ? y >> 1 : (y >> 1) - 1;
-        const float wlx = (x & 1) ? 0.75f : 0.25f, wly = (y & 1) ? 0.75f : 0.25f;
-        const int zc = (z0 >> 1) - 1;
-        float sum[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int o = 0; o < 4; o++) {
-            const int ox = o >> 1, oy = o & 1;
-            const int cx = px + ox, cy = py + oy;
-            if (cx < 0 || cy < 0 || cx >= Cl.nx || cy >= Cl.ny) continue;
-            const float wxy = (ox ? 1.f - wlx : wlx) * (oy ? 1.f - wly : wly);
-            const long long row = ((long long)cx * Cl.ny + cy) * Cl.pz;
-            float cv[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const int z = zc + k;
-                cv[k] = (z >= 0 && z < Cl.nz && (Cl.code[row + z] & CODE_FLUID)) ? Cl.x[row + z] : 0.f;
-            }
-            // lanes: z0 (lower zc, w 1/4), z0+1 (zc+1, 3/4), z0+2 (zc+1, 1/4), z0+3 (zc+2, 3/4)
-            sum[0] += wxy * (0.25f * cv[0] + 0.75f * cv[1]);
-            sum[1] += wxy * (0.75f * cv[1] + 0.25f * cv[2]);
-            sum[2] += wxy * (0.25f * cv[1] + 0.75f * cv[2]);
-            sum[3] += wxy * (0.75f * cv[2] + 0.25f * cv[3]);
-        }
-        float xv[4];
-        unpack4(ld4(F.x + c0), xv);
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-            if (cc[i] & CODE_FLUID) xv[i] += sum[i];
-        st4(F.x + c0, xv);
-    });
+    mg_for_quads<FINE>(A, F, [&](int x, int y, int z0, long long c0) { prolong_quad(F, Cl, x, y, z0, c0); });
 }
 
 // ---- MG-path PCG kernels on quads (level 0, FP32) ------------------------------
@@ -923,11 +942,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update_q(const PcgArgs a, Vecs<
 }
 
 // coarsest level: symmetric red-black Gauss-Seidel in shared memory, one CTA
-__global__ void __launch_bounds__(1024) k_mg_bottom(const PcgState* st, MGLev L) {
-    if (st->done) return;
-    __shared__ float sx[MG_BOTTOM_MAX];
-    __shared__ float sf[MG_BOTTOM_MAX];
-    __shared__ uint16_t sc[MG_BOTTOM_MAX];
+__device__ void mg_bottom_block(const MGLev& L, float* sx, float* sf, uint16_t* sc) {
     const int n = L.nx * L.ny * L.nz;  // dense in shared memory, padded in global
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const long long gi = (long long)(i / L.nz) * L.pz + (i % L.nz);
@@ -959,6 +974,79 @@ __global__ void __launch_bounds__(1024) k_mg_bottom(const PcgState* st, MGLev L)
         }
     }
     for (int i = threadIdx.x; i < n; i += blockDim.x) L.x[(long long)(i / L.nz) * L.pz + (i % L.nz)] = sx[i];
+}
+
+__global__ void __launch_bounds__(1024) k_mg_bottom(const PcgState* st, MGLev L) {
+    if (st->done) return;
+    __shared__ float sx[MG_BOTTOM_MAX];
+    __shared__ float sf[MG_BOTTOM_MAX];
+    __shared__ uint16_t sc[MG_BOTTOM_MAX];
+    mg_bottom_block(L, sx, sf, sc);
+}
+
+// The coarse part of the V-cycle in one launch: levels lc .. last (lc's rhs was
+// restricted by the caller) run by one thread-block cluster, the passes over a
+// level separated by cluster barriers (release/acquire at cluster scope, so
+// each pass sees the previous pass's global writes).  Replaces ~11 launches per
+// level of latency-bound small kernels.
+constexpr int MG_MAX_LEVELS = 12;
+constexpr int MG_CLUSTER_THREADS = 1024;
+constexpr long long MG_CLUSTER_CELLS = 300000;  // largest level handed to the cluster kernel
+
+struct MGChain {
+    MGLev lev[MG_MAX_LEVELS];
+    int lc, last, nu;
+};
+
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ unsigned cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cluster_size() {
+    unsigned n;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(n));
+    return n;
+}
+
+__global__ void __launch_bounds__(MG_CLUSTER_THREADS) k_mg_coarse(const PcgArgs A, const __grid_constant__ MGChain C) {
+    if (A.st->done) return;  // the same value in every CTA of the cluster
+    __shared__ float sx[MG_BOTTOM_MAX];
+    __shared__ float sf[MG_BOTTOM_MAX];
+    __shared__ uint16_t sc[MG_BOTTOM_MAX];
+    const long long i0 = (long long)cluster_rank() * blockDim.x + threadIdx.x;
+    const long long step = (long long)cluster_size() * blockDim.x;
+    for (int l = C.lc; l < C.last; l++) {
+        const MGLev& L = C.lev[l];
+        for (int k = 0; k < C.nu; k++) {
+            mg_for_range(L, i0, step, [&](int x, int y, int z0, long long c0) { smooth_quad(L, L.f, 0, k == 0, x, y, z0, c0); });
+            cluster_barrier();
+            mg_for_range(L, i0, step, [&](int x, int y, int z0, long long c0) { smooth_quad(L, L.f, 1, 0, x, y, z0, c0); });
+            cluster_barrier();
+        }
+        mg_for_range(L, i0, step, [&](int x, int y, int z0, long long c0) { residual_quad(L, L.f, x, y, z0, c0); });
+        cluster_barrier();
+        const MGLev& Cl = C.lev[l + 1];
+        mg_for_range(Cl, i0, step, [&](int x, int y, int z0, long long c0) { restrict_quad(L, Cl, x, y, z0, c0); });
+        cluster_barrier();
+    }
+    if (cluster_rank() == 0) mg_bottom_block(C.lev[C.last], sx, sf, sc);
+    cluster_barrier();
+    for (int l = C.last - 1; l >= C.lc; l--) {
+        const MGLev& L = C.lev[l];
+        const MGLev& Cl = C.lev[l + 1];
+        mg_for_range(L, i0, step, [&](int x, int y, int z0, long long c0) { prolong_quad(L, Cl, x, y, z0, c0); });
+        cluster_barrier();
+        for (int k = 0; k < C.nu; k++) {
+            mg_for_range(L, i0, step, [&](int x, int y, int z0, long long c0) { smooth_quad(L, L.f, 1, 0, x, y, z0, c0); });
+            cluster_barrier();
+            mg_for_range(L, i0, step, [&](int x, int y, int z0, long long c0) { smooth_quad(L, L.f, 0, 0, x, y, z0, c0); });
+            cluster_barrier();
+        }
+    }
 }
 
 // coarse cell kinds: fluid if any child is fluid, else air if any child is air
@@ -1098,6 +1186,31 @@ int solver_alloc(fsim_ctx* ctx) {
         ctx->err = "multigrid coarsest level too large";
         return FSIM_E_INVALID;
     }
+    // cluster for the coarse V-cycle: 16 CTAs where the GPU schedules them, else 8
+    S.mg_cluster = 0;
+    for (int cs : {16, 8}) {
+        if (cs > 8 && cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                          cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(MG_CLUSTER_THREADS);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, k_mg_coarse, &cfg) == cudaSuccess && nclusters > 0) {
+            S.mg_cluster = cs;
+            break;
+        }
+        cudaGetLastError();
+    }
     return FSIM_OK;
 }
 
@@ -1135,7 +1248,8 @@ static void mg_setup(fsim_ctx* ctx) {
 // last level-0 sweep also computes z.r and the CG scalars (k_red modes).
 static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, const float* r1, float* z,
                       bool first_fused, int dot_mode) {
-    const int NU = ctx->prm.mg_sweeps > 0 ? ctx->prm.mg_sweeps : MG_NU_DEFAULT;
+    const int NU0 = ctx->prm.mg_sweeps > 0 ? ctx->prm.mg_sweeps : MG_NU_DEFAULT;
+    const int NU = (l > 0 && ctx->prm.mg_coarse_sweeps > 0) ? ctx->prm.mg_coarse_sweeps : NU0;
     SolverBufs& S = ctx->sv;
     cudaStream_t st = ctx->stream;
     const int G = S.grid_blocks;
@@ -1143,6 +1257,27 @@ static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, c
     const int last = (int)S.mg.size() - 1;
     if (l == last) {
         k_mg_bottom<<<1, 1024, 0, st>>>(A.st, L);
+        ctx->launches += 1;
+        return;
+    }
+    if (l > 0 && S.mg_cluster > 0 && (long long)S.mg[l].ncell <= MG_CLUSTER_CELLS && last - l < MG_MAX_LEVELS) {
+        MGChain C{};
+        for (int k = l; k <= last; k++) C.lev[k - l] = mg_lev(S, k, nullptr, nullptr, nullptr);
+        C.lc = 0;
+        C.last = last - l;
+        C.nu = NU;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(S.mg_cluster);
+        cfg.blockDim = dim3(MG_CLUSTER_THREADS);
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = S.mg_cluster;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_mg_coarse, A, C);
         ctx->launches += 1;
         return;
     }
@@ -1297,7 +1432,7 @@ static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, int prec
         ctx->launches += 2;
         precondition(1, true);
     };
-    const int key = (int)sizeof(T) * 1000 + (mg ? 100 : 0) + ctx->prm.mg_sweeps;
+    const int key = (int)sizeof(T) * 100000 + (mg ? 10000 : 0) + ctx->prm.mg_sweeps * 100 + ctx->prm.mg_coarse_sweeps;
     if (S.iter_exec == nullptr || S.iter_key != key) {
         if (S.iter_exec) {
             cudaGraphExecDestroy(S.iter_exec);

@@ -173,3 +173,39 @@ def train(net: N.WarmStartNet, xs, ts, ms, *, iters: int, batch: int, lr: float 
         if log_every and it % log_every == 0:
             print(f"iter {it} loss {loss:.4e}", flush=True)
     return hist
+
+
+def time_forward(size: int, iters: int = 5, seed: int = 1):
+    """CUDA-event time of one network forward pass on a size^3 volume (random input)."""
+    import torch
+
+    net = N.WarmStartNet(seed=seed)
+    x = torch.zeros((1, size, size, size, 4), device="cuda")
+    x[..., 0] = torch.randn((1, size, size, size), device="cuda")
+    x[..., 1] = 1.0
+    net.forward(x)  # workspace allocation
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(iters):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        net.forward(x)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    net.close()
+    return times
+
+
+if __name__ == "__main__":
+    import argparse
+
+    ap = argparse.ArgumentParser(description="warm-start network utilities")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    f = sub.add_parser("forward", help="time the forward pass")
+    f.add_argument("--size", type=int, default=256)
+    f.add_argument("--iters", type=int, default=5)
+    a = ap.parse_args()
+    if a.cmd == "forward":
+        t = time_forward(a.size, a.iters)
+        print(f"forward {a.size}^3 ms: " + " ".join(f"{v:.3f}" for v in t), flush=True)

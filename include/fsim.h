@@ -155,7 +155,8 @@ typedef struct fsim_params {
     int timing;             /* record per-stage CUDA-event times into fsim_step_stats */
     int precond;            /* fsim_precond (FSIM_PREC_FP64 always uses FSIM_PRECOND_RBIC) */
     int mg_sweeps;          /* multigrid smoothing sweeps before and after the coarse correction (0: 2) */
-    int reserved[5];
+    int mg_coarse_sweeps;   /* the same on the coarser levels (0: as mg_sweeps) */
+    int reserved[4];
 } fsim_params;
 
 /* Obstacle (obstacles.hpp:7-65), speed set by the caller as (pos-prevPos)/dt. */
