@@ -216,7 +216,7 @@ def run_fsim(args):
     p = N.default_params(transfer=N.APIC, resolution=res, tol=1e-6, tol_mode=N.TOL_REL_L2, max_iters=2000,
                          spawning=True, despawning=True, timing=True, precision=N.PREC_MIXED,
                          warm_start=N.WARM_ZERO, precond=precond, mg_sweeps=args.mg_sweeps,
-                         mg_coarse_sweeps=args.mg_coarse_sweeps)
+                         mg_coarse_sweeps=args.mg_coarse_sweeps, mg_cluster_sweeps=args.mg_cluster_sweeps)
     sim = N.Simulation(res, p)
     sim.set_particles(pos)
     del pos
@@ -506,6 +506,8 @@ def main():
                     help="multigrid smoothing sweeps before and after the coarse correction (0: library default)")
     ap.add_argument("--mg-coarse-sweeps", type=int, default=0,
                     help="multigrid sweeps on the coarser levels (0: as --mg-sweeps)")
+    ap.add_argument("--mg-cluster-sweeps", type=int, default=0,
+                    help="multigrid sweeps on the levels run by the cluster kernel (0: library default)")
     ap.add_argument("--ws-steps", type=int, default=4,
                     help="problems of the zero / previous / learned warm-start comparison (0: skip)")
     ap.add_argument("--ws-problems", type=int, default=48, help="synthetic training problems at 64^3")

@@ -479,7 +479,13 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
 // correction and black->red after it; the coarsest level (<= 512 cells) is
 // smoothed BOTTOM times each way inside one CTA.  Starting every level from
 // zero, the V-cycle is a fixed symmetric linear operator, as CG requires.
-constexpr int MG_NU_DEFAULT = 2;
+// Sweeps per level group, measured on the 256^3 fill workload (PCG to 1e-6):
+// (2, 2, 2) took 30 iterations at 0.83 ms, (3, 6, 6) 16 iterations at 1.30 ms.
+// The coarse correction near the free surface is the weak part of the cycle,
+// so extra coarse smoothing pays for itself.
+constexpr int MG_NU_DEFAULT = 3;           // level 0
+constexpr int MG_NU_COARSE_DEFAULT = 6;    // level 1 and other separately launched levels
+constexpr int MG_NU_CLUSTER_DEFAULT = 6;   // levels run by the cluster kernel
 constexpr int MG_BOTTOM_SWEEPS = 12;
 constexpr int MG_BOTTOM_MAX = 4096;
 
@@ -1012,11 +1018,11 @@ __device__ __forceinline__ unsigned cluster_size() {
     return n;
 }
 
+constexpr int MG_POOL_FLOATS = (MG_BOTTOM_MAX * 5 + 1) / 2;  // bottom: x, f (floats) and codes
+
 __global__ void __launch_bounds__(MG_CLUSTER_THREADS) k_mg_coarse(const PcgArgs A, const __grid_constant__ MGChain C) {
     if (A.st->done) return;  // the same value in every CTA of the cluster
-    __shared__ float sx[MG_BOTTOM_MAX];
-    __shared__ float sf[MG_BOTTOM_MAX];
-    __shared__ uint16_t sc[MG_BOTTOM_MAX];
+    __shared__ float pool[MG_POOL_FLOATS];
     const long long i0 = (long long)cluster_rank() * blockDim.x + threadIdx.x;
     const long long step = (long long)cluster_size() * blockDim.x;
     for (int l = C.lc; l < C.last; l++) {
@@ -1033,7 +1039,8 @@ __global__ void __launch_bounds__(MG_CLUSTER_THREADS) k_mg_coarse(const PcgArgs 
         mg_for_range(Cl, i0, step, [&](int x, int y, int z0, long long c0) { restrict_quad(L, Cl, x, y, z0, c0); });
         cluster_barrier();
     }
-    if (cluster_rank() == 0) mg_bottom_block(C.lev[C.last], sx, sf, sc);
+    if (cluster_rank() == 0)
+        mg_bottom_block(C.lev[C.last], pool, pool + MG_BOTTOM_MAX, reinterpret_cast<uint16_t*>(pool + 2 * MG_BOTTOM_MAX));
     cluster_barrier();
     for (int l = C.last - 1; l >= C.lc; l--) {
         const MGLev& L = C.lev[l];
@@ -1248,8 +1255,11 @@ static void mg_setup(fsim_ctx* ctx) {
 // last level-0 sweep also computes z.r and the CG scalars (k_red modes).
 static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, const float* r1, float* z,
                       bool first_fused, int dot_mode) {
-    const int NU0 = ctx->prm.mg_sweeps > 0 ? ctx->prm.mg_sweeps : MG_NU_DEFAULT;
-    const int NU = (l > 0 && ctx->prm.mg_coarse_sweeps > 0) ? ctx->prm.mg_coarse_sweeps : NU0;
+    const fsim_params& P = ctx->prm;
+    const int NU0 = P.mg_sweeps > 0 ? P.mg_sweeps : MG_NU_DEFAULT;
+    const int NU1 = P.mg_coarse_sweeps > 0 ? P.mg_coarse_sweeps : MG_NU_COARSE_DEFAULT;
+    const int NUC = P.mg_cluster_sweeps > 0 ? P.mg_cluster_sweeps : MG_NU_CLUSTER_DEFAULT;
+    const int NU = l == 0 ? NU0 : NU1;
     SolverBufs& S = ctx->sv;
     cudaStream_t st = ctx->stream;
     const int G = S.grid_blocks;
@@ -1265,7 +1275,7 @@ static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, c
         for (int k = l; k <= last; k++) C.lev[k - l] = mg_lev(S, k, nullptr, nullptr, nullptr);
         C.lc = 0;
         C.last = last - l;
-        C.nu = NU;
+        C.nu = NUC;
         cudaLaunchConfig_t cfg{};
         cfg.gridDim = dim3(S.mg_cluster);
         cfg.blockDim = dim3(MG_CLUSTER_THREADS);
@@ -1432,7 +1442,8 @@ static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, int prec
         ctx->launches += 2;
         precondition(1, true);
     };
-    const int key = (int)sizeof(T) * 100000 + (mg ? 10000 : 0) + ctx->prm.mg_sweeps * 100 + ctx->prm.mg_coarse_sweeps;
+    const int key = (int)sizeof(T) * 10000000 + (mg ? 1000000 : 0) + ctx->prm.mg_sweeps * 10000 +
+                    ctx->prm.mg_coarse_sweeps * 100 + ctx->prm.mg_cluster_sweeps;
     if (S.iter_exec == nullptr || S.iter_key != key) {
         if (S.iter_exec) {
             cudaGraphExecDestroy(S.iter_exec);

@@ -46,7 +46,8 @@ class Params(C.Structure):
         ("max_iters", C.c_int), ("fluid_density", C.c_double), ("residual_tol", C.c_double),
         ("tol_mode", C.c_int), ("particle_r", C.c_double), ("precision", C.c_int),
         ("warm_start", C.c_int), ("track_ids", C.c_int), ("timing", C.c_int), ("precond", C.c_int),
-        ("mg_sweeps", C.c_int), ("mg_coarse_sweeps", C.c_int), ("reserved", C.c_int * 4),
+        ("mg_sweeps", C.c_int), ("mg_coarse_sweeps", C.c_int), ("mg_cluster_sweeps", C.c_int),
+        ("reserved", C.c_int * 3),
     ]
 
 
@@ -163,7 +164,7 @@ def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: 
                    despawning: bool = False, stop_particles: bool = False, gravity_enabled: bool = True,
                    pressure_enabled: bool = False, pressure_k: float = 2.0, average_pressure: float = 2.0,
                    fluid_density: float = 1.0, timing: bool = False, precond: int = PRECOND_MG,
-                   mg_sweeps: int = 0, mg_coarse_sweeps: int = 0) -> Params:
+                   mg_sweeps: int = 0, mg_coarse_sweeps: int = 0, mg_cluster_sweeps: int = 0) -> Params:
     """Parameters of the dam-break workloads (reference parameter names in fsim.h)."""
     p = Params()
     p.transfer = transfer
@@ -191,6 +192,7 @@ def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: 
     p.precond = precond
     p.mg_sweeps = mg_sweeps
     p.mg_coarse_sweeps = mg_coarse_sweeps
+    p.mg_cluster_sweeps = mg_cluster_sweeps
     return p
 
 

@@ -154,9 +154,11 @@ typedef struct fsim_params {
     int track_ids;          /* keep a stable id per particle (fsim_get_particles in id order) */
     int timing;             /* record per-stage CUDA-event times into fsim_step_stats */
     int precond;            /* fsim_precond (FSIM_PREC_FP64 always uses FSIM_PRECOND_RBIC) */
-    int mg_sweeps;          /* multigrid smoothing sweeps before and after the coarse correction (0: 2) */
-    int mg_coarse_sweeps;   /* the same on the coarser levels (0: as mg_sweeps) */
-    int reserved[4];
+    int mg_sweeps;          /* multigrid smoothing sweeps before and after the coarse correction on
+                               the finest level (0: 3) */
+    int mg_coarse_sweeps;   /* the same on level 1 and other levels run as separate kernels (0: 6) */
+    int mg_cluster_sweeps;  /* the same on the small levels run by one thread-block cluster (0: 6) */
+    int reserved[3];
 } fsim_params;
 
 /* Obstacle (obstacles.hpp:7-65), speed set by the caller as (pos-prevPos)/dt. */
