@@ -337,6 +337,8 @@ def run_fsim(args):
                 "steps": e2e_steps, "path": "fsim_step + fsim_fill_gfx(pinned host) per step"},
         "gpu_launches": int(sum(s.kernel_launches for s in stats)),
     }
+    if args.precision_study:
+        line["pcg_precision"] = precision_study(sim, dt, N)
     if args.ws_steps > 0:
         line["pcg_warm_start"] = warm_start_study(sim, dt, t, h, N, args)
     sim.close()
@@ -344,6 +346,29 @@ def run_fsim(args):
         line["cpu_baseline"] = cpu_baseline(res, dt)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- precision study
+def precision_study(sim, dt, N):
+    """The last step's pressure problem (256^3 rhs and cell types) solved in each
+    precision; errors against an FP64 PCG solution (RB-IC, FP64 vectors,
+    relative residual 1e-12), max over fluid cells relative to max |p|."""
+    flags = sim.grid(N.F_FLAGS)
+    rhs = sim.grid(N.F_DIVERGENCE).astype(np.float64)
+    fluid = flags == N.WATER
+    runs = [("fp64_rbic_1e-12", N.PREC_FP64, 1e-12), ("mixed_mg_1e-6", N.PREC_MIXED, 1e-6),
+            ("fp32_mg_1e-6", N.PREC_FP32, 1e-6), ("mixed_mg_1e-10", N.PREC_MIXED, 1e-10)]
+    out = {}
+    ref = None
+    for name, prec, tol in runs:
+        p, st = sim.solve_pressure(rhs, dt, precision=prec, tol_mode=N.TOL_REL_L2, tol=tol, max_iters=20000)
+        if ref is None:
+            ref = p
+        scale = max(np.abs(ref[fluid]).max(), 1e-300)
+        out[name] = {"iterations": st.pcg_iterations, "ms": round(st.ms_solve, 3),
+                     "residual_rel": st.residual_rel,
+                     "err_vs_fp64": float(np.abs(p - ref)[fluid].max() / scale)}
+    return out
 
 
 # ---------------------------------------------------------------- learned warm start
@@ -508,6 +533,8 @@ def main():
                     help="multigrid sweeps on the coarser levels (0: as --mg-sweeps)")
     ap.add_argument("--mg-cluster-sweeps", type=int, default=0,
                     help="multigrid sweeps on the levels run by the cluster kernel (0: library default)")
+    ap.add_argument("--precision-study", type=int, default=1,
+                    help="solve the last step's pressure problem in FP64 / mixed / FP32 and report errors (0: skip)")
     ap.add_argument("--ws-steps", type=int, default=4,
                     help="problems of the zero / previous / learned warm-start comparison (0: skip)")
     ap.add_argument("--ws-problems", type=int, default=48, help="synthetic training problems at 64^3")

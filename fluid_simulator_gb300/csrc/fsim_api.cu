@@ -636,6 +636,11 @@ int fsim_stage(fsim_ctx* ctx, int stage, double dt, fsim_step_stats* stats) {
         case FSIM_STAGE_SOLVE: {
             fsim_step_stats tmp{};
             fsim_step_stats* sp = stats ? stats : &tmp;
+            if (P.grid_solver == FSIM_SOLVER_SOR) {
+                sp->pcg_iterations = launch_sor(ctx, P.max_iters);
+                CHECK_LAUNCH(ctx);
+                break;
+            }
             rc = solve_pressure(ctx, dt, P.precision, P.tol_mode, P.residual_tol, P.max_iters, P.warm_start, sp,
                                 nullptr, 1);
             break;
@@ -690,8 +695,14 @@ int fsim_step(fsim_ctx* ctx, double dt, fsim_step_stats* stats) {
     launch_prep(ctx, 1, 1, P.gravity_enabled ? (float)((double)P.gravity * dt) : 0.f);
     CHECK_LAUNCH(ctx);
     fsim_record(ctx, EV_PREP);
-    rc = solve_pressure(ctx, dt, P.precision, P.tol_mode, P.residual_tol, P.max_iters, P.warm_start, &st, nullptr, 1);
-    if (rc) return rc;
+    if (P.grid_solver == FSIM_SOLVER_SOR) {
+        st.pcg_iterations = launch_sor(ctx, P.max_iters);  // BasicMacGrid returns its iteration count
+        CHECK_LAUNCH(ctx);
+    } else {
+        rc = solve_pressure(ctx, dt, P.precision, P.tol_mode, P.residual_tol, P.max_iters, P.warm_start, &st,
+                            nullptr, 1);
+        if (rc) return rc;
+    }
     fsim_record(ctx, EV_SOLVE);
     launch_extrapolate(ctx);
     CHECK_LAUNCH(ctx);

@@ -167,6 +167,7 @@ int launch_obstacle(fsim_ctx* ctx, const fsim_obstacle& o);  // returns kernels 
 void launch_prep(fsim_ctx* ctx, int walls, int post, float gravity_inc);
 void launch_extrapolate(fsim_ctx* ctx);
 void launch_apply_pressure(fsim_ctx* ctx, double dt);
+int launch_sor(fsim_ctx* ctx, int iters);  // BasicMacGrid solver; returns the sweeps run
 void launch_pad_to_dense(const GridGeom& g, const void* src, void* dst, int elem, cudaStream_t s);
 void launch_dense_to_pad(const GridGeom& g, const void* src, void* dst, int elem, cudaStream_t s);
 void launch_counts(const GridGeom& g, const int* cstart, int* out, cudaStream_t s);

@@ -171,6 +171,41 @@ __global__ void k_extrapolate(GridGeom g, int it, const uint8_t* flags, uint8_t*
 // Each cell updates its own three faces: a fluid cell with a non-SOLID +a
 // neighbour adds scale*(p_c - p_n) (p_n = 0 for AIR); an AIR cell with a fluid
 // +a neighbour subtracts scale*p_n.
+// BasicMacGrid::solveIncompressibilityParallel (basicMacGrid.cpp:16-88): one
+// colour of the red-black SOR.  A WATER cell with s non-solid neighbours
+// spreads d = 1.98 (-div v2 [+ density term]) / s over its six faces (a face
+// towards a SOLID neighbour stays).  Cells of one colour share no face, so the
+// update is order-free and deterministic.  parity: (x + y + z) & 1 of the
+// colour (the reference runs odd, then even).
+__global__ void k_sor(GridGeom g, const uint8_t* flags, float* vx, float* vy, float* vz, const float* avg,
+                      int pressure_enabled, float avg_pressure, float pressure_k, int parity, float omega) {
+    const int ix = (g.nx - 2), iy = (g.ny - 2), izh = (g.nz - 1) / 2;  // z pairs per interior row
+    const long long total = (long long)ix * iy * izh;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int x = 1 + (int)(t / ((long long)iy * izh));
+    const int y = 1 + (int)((t / izh) % iy);
+    const int z = 1 + ((x + y + 1 + parity) & 1) + 2 * (int)(t % izh);
+    if (z >= g.nz - 1) return;
+    const long long c = gidx(g, x, y, z);
+    if (flags[c] != C_WATER) return;
+    const long long sx = (long long)g.pz * g.ny, sy = g.pz;
+    const int s1 = flags[c + 1] != C_SOLID, s2 = flags[c - 1] != C_SOLID;
+    const int s3 = flags[c + sy] != C_SOLID, s4 = flags[c - sy] != C_SOLID;
+    const int s5 = flags[c + sx] != C_SOLID, s6 = flags[c - sx] != C_SOLID;
+    const int s = s1 + s2 + s3 + s4 + s5 + s6;
+    if (s == 0) return;
+    float d = -vx[c] - vy[c] - vz[c] + vx[c - sx] + vy[c - sy] + vz[c - 1];
+    if (pressure_enabled) d += (avg[c] - avg_pressure) * pressure_k;
+    d = d * omega / (float)s;
+    if (s1) vz[c] += d;
+    if (s2) vz[c - 1] -= d;
+    if (s3) vy[c] += d;
+    if (s4) vy[c - sy] -= d;
+    if (s5) vx[c] += d;
+    if (s6) vx[c - sx] -= d;
+}
+
 __global__ void k_apply_pressure(GridGeom g, const uint8_t* flags, const double* p, double scale,
                                  float* v0, float* v1, float* v2) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -292,6 +327,22 @@ void launch_extrapolate(fsim_ctx* ctx) {
     for (int it = 0; it < 2; it++)
         k_extrapolate<<<ceil_div(g.ncell, 256), 256, 0, ctx->stream>>>(g, it, ctx->flags, ctx->valid,
                                                                        ctx->v2[0], ctx->v2[1], ctx->v2[2]);
+}
+
+int launch_sor(fsim_ctx* ctx, int iters) {
+    const GridGeom& g = ctx->g;
+    if (g.nx < 3 || g.ny < 3 || g.nz < 3) return 0;
+    const long long total = (long long)(g.nx - 2) * (g.ny - 2) * ((g.nz - 1) / 2);
+    const fsim_params& P = ctx->prm;
+    for (int n = 0; n < iters; n++) {
+        for (int parity = 1; parity >= 0; parity--)
+            k_sor<<<ceil_div(total, 256), 256, 0, ctx->stream>>>(g, ctx->flags, ctx->v2[0], ctx->v2[1], ctx->v2[2],
+                                                                  ctx->avg, P.pressure_enabled,
+                                                                  (float)P.average_pressure, (float)P.pressure_k,
+                                                                  parity, 1.98f);
+    }
+    ctx->launches += 2LL * iters;
+    return iters;
 }
 
 void launch_apply_pressure(fsim_ctx* ctx, double dt) {

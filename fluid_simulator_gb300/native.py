@@ -24,6 +24,7 @@ TOL_ABS_MAX, TOL_REL_L2 = 0, 1
 PREC_MIXED, PREC_FP32, PREC_FP64 = 0, 1, 2
 WARM_ZERO, WARM_PREVIOUS, WARM_GUESS, WARM_LEARNED = 0, 1, 2, 3
 PRECOND_RBIC, PRECOND_MG = 0, 1
+SOLVER_PCG, SOLVER_SOR = 0, 1
 (STAGE_SPAWN, STAGE_ADVECT, STAGE_PUSH_APART, STAGE_PUSH_OUT, STAGE_STOP, STAGE_P2G, STAGE_MARK,
  STAGE_OBSTACLES, STAGE_WALLS, STAGE_POST_P2G, STAGE_SOLVE, STAGE_EXTRAPOLATE, STAGE_G2P) = range(13)
 (F_FLAGS, F_AVGPNUM, F_VX, F_VY, F_VZ, F_V2X, F_V2Y, F_V2Z, F_PRESSURE, F_COUNT,
@@ -47,7 +48,7 @@ class Params(C.Structure):
         ("tol_mode", C.c_int), ("particle_r", C.c_double), ("precision", C.c_int),
         ("warm_start", C.c_int), ("track_ids", C.c_int), ("timing", C.c_int), ("precond", C.c_int),
         ("mg_sweeps", C.c_int), ("mg_coarse_sweeps", C.c_int), ("mg_cluster_sweeps", C.c_int),
-        ("reserved", C.c_int * 3),
+        ("grid_solver", C.c_int), ("reserved", C.c_int * 2),
     ]
 
 
@@ -164,7 +165,8 @@ def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: 
                    despawning: bool = False, stop_particles: bool = False, gravity_enabled: bool = True,
                    pressure_enabled: bool = False, pressure_k: float = 2.0, average_pressure: float = 2.0,
                    fluid_density: float = 1.0, timing: bool = False, precond: int = PRECOND_MG,
-                   mg_sweeps: int = 0, mg_coarse_sweeps: int = 0, mg_cluster_sweeps: int = 0) -> Params:
+                   mg_sweeps: int = 0, mg_coarse_sweeps: int = 0, mg_cluster_sweeps: int = 0,
+                   grid_solver: int = SOLVER_PCG) -> Params:
     """Parameters of the dam-break workloads (reference parameter names in fsim.h)."""
     p = Params()
     p.transfer = transfer
@@ -193,6 +195,7 @@ def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: 
     p.mg_sweeps = mg_sweeps
     p.mg_coarse_sweeps = mg_coarse_sweeps
     p.mg_cluster_sweeps = mg_cluster_sweeps
+    p.grid_solver = grid_solver
     return p
 
 

@@ -80,6 +80,13 @@ enum fsim_precond {
     FSIM_PRECOND_MG = 1    /* geometric multigrid V-cycle (red-black Gauss-Seidel smoothing) */
 };
 
+/* Incompressibility solver, SimulationConfig::gridSolverType (simulationManager.cpp:16-19). */
+enum fsim_grid_solver {
+    FSIM_SOLVER_PCG = 0, /* BridsonSolverGrid: pressure PCG (bridsonSolverGrid.cpp:244-293) */
+    FSIM_SOLVER_SOR = 1  /* BasicMacGrid: max_iters red-black SOR sweeps on the face velocities,
+                            over-relaxation 1.98 (basicMacGrid.cpp:5-88) */
+};
+
 /* Initial guess of the pressure solve. */
 enum fsim_warm_start {
     FSIM_WARM_ZERO = 0,     /* p0 = 0, as the reference */
@@ -158,7 +165,8 @@ typedef struct fsim_params {
                                the finest level (0: 3) */
     int mg_coarse_sweeps;   /* the same on level 1 and other levels run as separate kernels (0: 6) */
     int mg_cluster_sweeps;  /* the same on the small levels run by one thread-block cluster (0: 6) */
-    int reserved[3];
+    int grid_solver;        /* fsim_grid_solver: SimulationConfig::gridSolverType */
+    int reserved[2];
 } fsim_params;
 
 /* Obstacle (obstacles.hpp:7-65), speed set by the caller as (pos-prevPos)/dt. */

@@ -23,7 +23,7 @@
 // Parts of the reference interface that only the reference's own Simulator
 // uses internally (face/cell stencil helpers, grid reset, P2G helpers, the
 // intersection hash) are not declared; pushParticlesApart throws, as the GPU
-// library does not build it.  Default particle positions of HashedParticles
+// library does not build it.  BasicMacGrid selects the library's SOR solver.  Default particle positions of HashedParticles
 // use a SplitMix64 generator instead of std::rand.
 //
 // Requires glm (glm::dvec3, glm::ivec3) and C++17.
@@ -472,6 +472,21 @@ public:
     }
 };
 
+// Reference: basicMacGrid.h:7-17 -- the SOR solver, selected by the manager for
+// SimulationConfig::GridSolverType::BASIC (simulationManager.cpp:16-19).
+class BasicMacGrid : public MacGrid {
+public:
+    using MacGrid::MacGrid;
+
+    int solveIncompressibility(bool /*parallel*/, double dt) override {
+        if (!device) throw std::runtime_error("solveIncompressibility: the grid is not bound to a Simulator");
+        fsim_step_stats st{};
+        facade_detail::check(fsim_stage(device, FSIM_STAGE_SOLVE, dt, &st), device, "fsim_stage(SOLVE)");
+        host_valid = false;
+        return st.pcg_iterations;
+    }
+};
+
 }  // namespace macgrid
 
 // ---------------------------------------------------------------- simulator
@@ -593,6 +608,7 @@ private:
         p.track_ids = 0;
         p.timing = 1;
         p.precond = FSIM_PRECOND_MG;
+        p.grid_solver = dynamic_cast<const macgrid::BasicMacGrid*>(&g) ? FSIM_SOLVER_SOR : FSIM_SOLVER_PCG;
         return p;
     }
 

@@ -802,6 +802,45 @@ static double dotp(const double *a, const double *b, int n) {
  * calculatePreconditioner (:91-124, tau 0.97, sigma 0.25) and
  * applyPressureToVelocities (:295-327).  PCG starts from zero pressure and stops
  * on the absolute max-norm of the recursive residual. */
+/* BasicMacGrid::solveIncompressibilityParallel (basicMacGrid.cpp:16-88), the
+ * release-build path: max_iters times, every odd-parity WATER cell, then every
+ * even one, spreads d = 1.98 (-div v2 [+ density term]) / s over its six faces
+ * (s = non-SOLID neighbours; faces towards SOLID neighbours stay).  Cells of
+ * one parity share no face, so the result does not depend on the loop order. */
+static int stage_sor(sim *s) {
+    const double omega = 1.98;
+    const int yz = s->yz, nz = s->nz;
+    for (int n = 0; n < s->p.max_iters; n++) {
+        for (int par = 1; par >= 0; par--) {
+#pragma omp parallel for schedule(static)
+            for (int x = 1; x < s->nx - 1; x++)
+                for (int y = 1; y < s->ny - 1; y++)
+                    for (int z = 1; z < nz - 1; z++) {
+                        if (((x + y + z) & 1) != par) continue;
+                        const int c = x * yz + y * nz + z;
+                        if (s->type[c] != ORACLE_WATER) continue;
+                        const int s1 = s->type[c + 1] != ORACLE_SOLID, s2 = s->type[c - 1] != ORACLE_SOLID;
+                        const int s3 = s->type[c + nz] != ORACLE_SOLID, s4 = s->type[c - nz] != ORACLE_SOLID;
+                        const int s5 = s->type[c + yz] != ORACLE_SOLID, s6 = s->type[c - yz] != ORACLE_SOLID;
+                        const int ssum = s1 + s2 + s3 + s4 + s5 + s6;
+                        if (ssum == 0) continue;
+                        double d = -s->v2[0][c] - s->v2[1][c] - s->v2[2][c] + s->v2[0][c - yz] + s->v2[1][c - nz] +
+                                   s->v2[2][c - 1] +
+                                   (s->p.pressure_enabled ? (s->avg[c] - s->p.average_pressure) * s->p.pressure_k : 0.0);
+                        d = d * omega / ssum;
+                        if (s1) s->v2[2][c] += d;
+                        if (s2) s->v2[2][c - 1] -= d;
+                        if (s3) s->v2[1][c] += d;
+                        if (s4) s->v2[1][c - nz] -= d;
+                        if (s5) s->v2[0][c] += d;
+                        if (s6) s->v2[0][c - yz] -= d;
+                    }
+        }
+    }
+    s->last_its = s->p.max_iters;
+    return s->p.max_iters;
+}
+
 static int stage_solve(sim *s, double dt) {
     const int nf = s->nfluid;
     const double tau = 0.97, sig = 0.25;
@@ -1014,7 +1053,7 @@ int oracle_stage(void *h, int stage, double dt) {
         case ORACLE_STAGE_POST_P2G:
             stage_post_p2g(s, s->p.gravity_enabled ? (double)s->p.gravity * dt : 0.0);
             return 0;
-        case ORACLE_STAGE_SOLVE: return stage_solve(s, dt);
+        case ORACLE_STAGE_SOLVE: return s->p.grid_solver == 1 ? stage_sor(s) : stage_solve(s, dt);
         case ORACLE_STAGE_EXTRAPOLATE: stage_extrapolate(s); return 0;
         case ORACLE_STAGE_G2P: stage_g2p(s); return 0;
         default: return -1;
@@ -1033,7 +1072,7 @@ int oracle_step(void *h, double dt) {
     stage_obstacles(s);
     walls(s);
     stage_post_p2g(s, s->p.gravity_enabled ? (double)s->p.gravity * dt : 0.0);
-    int its = stage_solve(s, dt);
+    int its = s->p.grid_solver == 1 ? stage_sor(s) : stage_solve(s, dt);
     stage_extrapolate(s);
     stage_g2p(s);
     return its;

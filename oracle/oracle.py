@@ -58,6 +58,7 @@ class OracleParams(C.Structure):
         ("average_pressure", C.c_double),
         ("fluid_density", C.c_double),
         ("residual_tol", C.c_double),
+        ("grid_solver", C.c_int),
     ]
 
 
@@ -138,7 +139,7 @@ def make_params(resolution: float, *, transfer: int = FLIP, flip_ratio: float = 
                 gravity_enabled: bool = True, spawning: bool = False, despawning: bool = False,
                 stop_particles: bool = False, pressure_enabled: bool = False,
                 pressure_k: float = 2.0, average_pressure: float = 2.0,
-                fluid_density: float = 1.0, two_d: bool = False) -> OracleParams:
+                fluid_density: float = 1.0, two_d: bool = False, grid_solver: int = 0) -> OracleParams:
     p = OracleParams()
     p.resolution = resolution
     p.dims[:] = list(dims)
@@ -159,6 +160,7 @@ def make_params(resolution: float, *, transfer: int = FLIP, flip_ratio: float = 
     p.average_pressure = average_pressure
     p.fluid_density = fluid_density
     p.residual_tol = tol
+    p.grid_solver = grid_solver
     return p
 
 

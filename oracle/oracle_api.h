@@ -63,6 +63,8 @@ typedef struct oracle_params {
     double average_pressure;
     double fluid_density;
     double residual_tol;        /* MacGrid::residualTolerance (absolute max-norm) */
+    int grid_solver;            /* 0 BridsonSolverGrid (PCG), 1 BasicMacGrid (SOR) --
+                                   SimulationConfig::gridSolverType (simulationManager.cpp:16-19) */
 } oracle_params;
 
 typedef struct oracle_obstacle {

@@ -41,6 +41,7 @@
 #define protected public
 #include "simulator/simulator.h"
 #include "simulator/macGrid/bridsonSolverGrid.h"
+#include "simulator/macGrid/basicMacGrid.h"
 #include "simulator/particles/hashedParticles.h"
 #include "simulator/macGrid/obstacles.hpp"
 #undef private
@@ -55,12 +56,37 @@ namespace {
 class ProbeGrid : public macgrid::BridsonSolverGrid {
 public:
     ProbeGrid(const glm::dvec3& dims, float res, bool twoD, double rho)
-        : macgrid::BridsonSolverGrid(dims, res, twoD, rho) {}
+        : macgrid::BridsonSolverGrid(dims, res, twoD, rho), dims0(dims), res0(res) {}
+
+    glm::dvec3 dims0;  // constructor arguments, to build an identical BasicMacGrid
+    double res0;
 
     std::vector<double> pressure;
     int lastIterations = 0;
+    int gridSolver = 0;  // 1: run the reference's BasicMacGrid SOR instead
+
+    // BasicMacGrid::solveIncompressibility (basicMacGrid.cpp:5-12) on a copy of
+    // this grid's cell types, v2 and densities; v2 comes back
+    int solveBasic(bool parallel, double dt) {
+        macgrid::BasicMacGrid basic(dims0, res0, twoD);
+        basic.pressureEnabled = pressureEnabled;
+        basic.pressureK = pressureK;
+        basic.averagePressure = averagePressure;
+        basic.incompressibilityMaxIterationCount = incompressibilityMaxIterationCount;
+        for (int i = 0; i < cellCount; i++) {
+            basic.rawCells[i].type = rawCells[i].type;
+            basic.rawCells[i].avgPNum = rawCells[i].avgPNum.load();
+            for (int a = 0; a < 3; a++) basic.rawCells[i].faces[a].v2 = rawCells[i].faces[a].v2;
+        }
+        const int its = basic.solveIncompressibility(parallel, dt);
+        for (int i = 0; i < cellCount; i++)
+            for (int a = 0; a < 3; a++) rawCells[i].faces[a].v2 = basic.rawCells[i].faces[a].v2;
+        pressure.assign(cellCount, 0.0);
+        return its;
+    }
 
     int solveIncompressibility(bool parallel, double dt) override {
+        if (gridSolver == 1) return lastIterations = solveBasic(parallel, dt);
         const int n = cellCount;
         std::vector<double> before[3];
         for (int a = 0; a < 3; a++) {
@@ -173,6 +199,7 @@ void applyGridParams(Handle* h) {
     h->grid->pressureEnabled = p->pressure_enabled != 0;
     h->grid->fluidDensity = p->fluid_density;
     h->grid->residualTolerance = p->residual_tol;
+    h->grid->gridSolver = p->grid_solver;
 }
 
 void writeParticles(Handle* h, int n, const double* pos, const double* vel, const double* c) {

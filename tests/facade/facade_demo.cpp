@@ -4,13 +4,16 @@
 // obstacles, call simulate(dt) K times, read the particles back through
 // getParticleAt.  Input / output: raw float32 arrays (pos n x 3).
 //
-//   facade_demo <resolution> <steps> <dt> <transfer 0|1|2> <in_pos.bin> <out.bin>
+//   facade_demo <resolution> <steps> <dt> <transfer 0|1|2> <in_pos.bin> <out.bin> [basic]
+//
+// With "basic", the grid is a BasicMacGrid (the SOR solver).
 //
 // out.bin: int64 n, then pos (n x 3), v (n x 3), c (n x 9) as float32, then
 // int32 PCG iterations of the last step.
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
+#include <string>
 #include <iostream>
 #include <vector>
 
@@ -19,10 +22,11 @@
 using namespace genericfsim;
 
 int main(int argc, char** argv) {
-    if (argc != 7) {
-        std::cerr << "usage: facade_demo res steps dt transfer in_pos.bin out.bin\n";
+    if (argc != 7 && argc != 8) {
+        std::cerr << "usage: facade_demo res steps dt transfer in_pos.bin out.bin [basic]\n";
         return 2;
     }
+    const bool basic = argc == 8 && std::string(argv[7]) == "basic";
     const double res = std::atof(argv[1]);
     const int steps = std::atoi(argv[2]);
     const double dt = std::atof(argv[3]);
@@ -34,7 +38,9 @@ int main(int argc, char** argv) {
     in.read(reinterpret_cast<char*>(pos.data()), bytes);
     const size_t n = pos.size() / 3;
     try {
-        auto grid = std::make_shared<macgrid::BridsonSolverGrid>(glm::dvec3(1, 1, 1), (float)res, false, 1.0);
+        std::shared_ptr<macgrid::MacGrid> grid;
+        if (basic) grid = std::make_shared<macgrid::BasicMacGrid>(glm::dvec3(1, 1, 1), res, false);
+        else grid = std::make_shared<macgrid::BridsonSolverGrid>(glm::dvec3(1, 1, 1), (float)res, false, 1.0);
         grid->isTopOfContainerSolid = true;
         grid->pressureEnabled = false;
         grid->incompressibilityMaxIterationCount = 200;

@@ -27,8 +27,8 @@ def test_facade_compiles():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("transfer", [1, 2])
-def test_facade_matches_c_abi(gpu, tmp_path, transfer):
+@pytest.mark.parametrize("transfer,basic", [(1, False), (2, False), (1, True)])
+def test_facade_matches_c_abi(gpu, tmp_path, transfer, basic):
     from fluid_simulator_gb300 import native as N
     from fluid_simulator_gb300.scenes import GridSpec, dam_break
 
@@ -42,8 +42,8 @@ def test_facade_matches_c_abi(gpu, tmp_path, transfer):
     inp = tmp_path / "pos.bin"
     out = tmp_path / "out.bin"
     pos.astype(np.float32).tofile(inp)
-    r = subprocess.run([str(exe), str(res), str(steps), repr(dt), str(transfer), str(inp), str(out)],
-                       capture_output=True, text=True, timeout=300)
+    r = subprocess.run([str(exe), str(res), str(steps), repr(dt), str(transfer), str(inp), str(out)] +
+                       (["basic"] if basic else []), capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr + r.stdout
     raw = out.read_bytes()
     n = int(np.frombuffer(raw[:8], np.int64)[0])
@@ -55,7 +55,7 @@ def test_facade_matches_c_abi(gpu, tmp_path, transfer):
     p = N.default_params(transfer=transfer, resolution=res, flip_ratio=0.95, gravity=-9.81, max_iters=200,
                          tol=1e-6, tol_mode=N.TOL_ABS_MAX, precision=N.PREC_MIXED, warm_start=N.WARM_ZERO,
                          top_solid=True, particle_r=h / 4, pressure_enabled=False, timing=True,
-                         precond=N.PRECOND_MG)
+                         precond=N.PRECOND_MG, grid_solver=N.SOLVER_SOR if basic else N.SOLVER_PCG)
     sim = N.Simulation(res, p)
     sim.set_particles(pos)
     st = None

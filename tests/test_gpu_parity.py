@@ -91,6 +91,23 @@ def test_pressure_matches_oracle(gpu, port_lib, precision, precond):
         assert_close_field(g.grid(fg), o.grid(fo), REL_GRID * 10, f"v2 after projection {fg}")
 
 
+@pytest.mark.parametrize("pressure_enabled", [False, True])
+def test_sor_matches_oracle(gpu, port_lib, pressure_enabled):
+    """BasicMacGrid's SOR (FSIM_SOLVER_SOR) from identical flags, v2 and densities."""
+    pos, vel, c = moving_state(32, N.FLIP)
+    g, o = make_pair(pos, 32, N.FLIP, vel=vel, threads=4, max_iters=30, grid_solver=N.SOLVER_SOR,
+                     pressure_enabled=pressure_enabled)
+    g.stage(N.STAGE_P2G, DT32)
+    for st in (O.STAGE_P2G, O.STAGE_MARK, O.STAGE_OBSTACLES, O.STAGE_WALLS, O.STAGE_POST_P2G):
+        o.stage(st, DT32)
+    inject_grid_from_oracle(g, o, [N.F_FLAGS, N.F_AVGPNUM, N.F_V2X, N.F_V2Y, N.F_V2Z])
+    st = g.stage(N.STAGE_SOLVE, DT32)
+    assert st.pcg_iterations == 30 and o.stage(O.STAGE_SOLVE, DT32) == 30
+    # FP32 against FP64 over 30 over-relaxed sweeps
+    for fg, fo in ((N.F_V2X, O.F_V2X), (N.F_V2Y, O.F_V2Y), (N.F_V2Z, O.F_V2Z)):
+        assert_close_field(g.grid(fg), o.grid(fo), 1e-4, f"v2 after SOR {fg}")
+
+
 def test_multigrid_needs_far_fewer_iterations(gpu, port_lib):
     """Both preconditioners reach the same pressure; multigrid in far fewer iterations."""
     pos, vel, c = moving_state(32, N.FLIP)

@@ -90,6 +90,28 @@ def test_oracle_equals_reference_stagewise(port_lib, transfer):
             assert np.allclose(pr_a[m], pr_b[m], rtol=0, atol=1e-9 * np.abs(pr_b).max())
 
 
+@pytest.mark.skipif(not O.have_ref(), reason="reference library not built here")
+@pytest.mark.parametrize("pressure_enabled", [False, True])
+def test_sor_oracle_equals_reference(port_lib, pressure_enabled):
+    """BasicMacGrid's SOR: the oracle equals the reference's own solver bit for bit."""
+    from fluid_simulator_gb300.scenes import GridSpec, dam_break
+
+    pos = dam_break(GridSpec(32), (0, 0, 0), (0.5, 0.7, 1.0), seed=7).astype(np.float64)
+    p = O.make_params(32, transfer=O.FLIP, max_iters=25, grid_solver=1, pressure_enabled=pressure_enabled)
+    a = O.Oracle(p, pos, lib="ref")
+    b = O.Oracle(p, pos, lib="port")
+    dt = 1 / 120
+    for _ in range(3):
+        assert a.step(dt) == b.step(dt) == 25
+    for st in (O.STAGE_ADVECT, O.STAGE_PUSH_OUT, O.STAGE_P2G, O.STAGE_MARK, O.STAGE_OBSTACLES, O.STAGE_WALLS,
+               O.STAGE_POST_P2G, O.STAGE_SOLVE):
+        assert a.stage(st, dt) == b.stage(st, dt)
+    for f in (O.F_FLAGS, O.F_V2X, O.F_V2Y, O.F_V2Z):
+        assert np.array_equal(a.grid(f), b.grid(f)), f
+    for x, y in zip(a.particles(), b.particles()):
+        assert np.array_equal(x, y)
+
+
 def test_oracle_threads_agree_within_rounding(port_lib):
     """Multi-threaded oracle (timed CPU baseline) differs only by summation order."""
     from fluid_simulator_gb300.scenes import GridSpec, dam_break
