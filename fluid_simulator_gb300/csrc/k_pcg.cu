@@ -38,7 +38,34 @@
 #include "fsim_ctx.h"
 #include "fsim_net.h"
 
+#include <utility>
+
 namespace {
+
+// Programmatic dependent launch: the kernels of one PCG iteration are launched
+// with programmatic stream serialisation, so each grid is scheduled while its
+// predecessor drains.  Every such kernel lets its successor launch at once and
+// then waits for its predecessor's completion (and memory) before touching any
+// data, so the ordering of the stream is unchanged.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kern)(KArgs...), unsigned grid, unsigned block, cudaStream_t st, Args&&... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 constexpr int BRX = 2, BRY = 4, BRZ = 32;
 constexpr int PCG_THREADS = 256;
@@ -631,6 +658,7 @@ __device__ __forceinline__ void smooth_quad(const MGLev& L, const float* rhs, in
 
 template <bool FINE>
 __global__ void __launch_bounds__(PCG_THREADS) k_mg_smooth(const PcgArgs A, MGLev L, int color, int first) {
+    pdl_enter();
     if (A.st->done) return;
     const float* rhs = mg_rhs(A, L);
     mg_for_quads<FINE>(A, L, [&](int x, int y, int z0, long long c0) { smooth_quad(L, rhs, color, first, x, y, z0, c0); });
@@ -639,6 +667,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_mg_smooth(const PcgArgs A, MGLe
 // the last post-smoothing half sweep (red, level 0) fused with z.r (modes 0/1 as k_red)
 __global__ void __launch_bounds__(PCG_THREADS) k_mg_smooth_dot(const PcgArgs A, MGLev L, int mode) {
     __shared__ double scratch[32];
+    pdl_enter();
     if (A.st->done) return;
     const float* rhs = mg_rhs(A, L);
     Acc<float> zr;
@@ -699,6 +728,7 @@ __device__ __forceinline__ void residual_quad(const MGLev& L, const float* rhs, 
 
 template <bool FINE>
 __global__ void __launch_bounds__(PCG_THREADS) k_mg_residual(const PcgArgs A, MGLev L) {
+    pdl_enter();
     if (A.st->done) return;
     const float* rhs = mg_rhs(A, L);
     mg_for_quads<FINE>(A, L, [&](int x, int y, int z0, long long c0) { residual_quad(L, rhs, x, y, z0, c0); });
@@ -758,6 +788,7 @@ __device__ __forceinline__ void restrict_quad(const MGLev& F, const MGLev& Cl, i
 }
 
 __global__ void __launch_bounds__(PCG_THREADS) k_mg_restrict(const PcgState* st, MGLev F, MGLev Cl) {
+    pdl_enter();
     if (st->done) return;
     mg_for_range(Cl, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x,
                  [&](int x, int y, int z0, long long c0) { restrict_quad(F, Cl, x, y, z0, c0); });
@@ -803,6 +834,7 @@ __device__ __forceinline__ void prolong_quad(const MGLev& F, const MGLev& Cl, in
 
 template <bool FINE>
 __global__ void __launch_bounds__(PCG_THREADS) k_mg_prolong(const PcgArgs A, MGLev F, MGLev Cl) {
+    pdl_enter();
     if (A.st->done) return;
     mg_for_quads<FINE>(A, F, [&](int x, int y, int z0, long long c0) { prolong_quad(F, Cl, x, y, z0, c0); });
 }
@@ -811,6 +843,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_mg_prolong(const PcgArgs A, MGL
 // s_new = z + beta s_old; q = A' s_new; alpha = sigma / (s.q)
 __global__ void __launch_bounds__(PCG_THREADS) k_spmv_q(const PcgArgs a, Vecs<float> v, MGLev L) {
     __shared__ double scratch[32];
+    pdl_enter();
     if (a.st->done) return;
     const int sc = (a.st->bufsel >> 1) & 1;
     const float beta = (float)a.st->beta;
@@ -868,6 +901,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_spmv_q(const PcgArgs a, Vecs<fl
 // V-cycle from zero on r_new (red z = r/ns, black z = (r + sum_j r_j/ns_j)/ns)
 __global__ void __launch_bounds__(PCG_THREADS) k_update_q(const PcgArgs a, Vecs<float> v, MGLev L) {
     __shared__ double scratch[32 * 2];
+    pdl_enter();
     if (a.st->done) return;
     const int rc = a.st->bufsel & 1, sc = (a.st->bufsel >> 1) & 1;
     const float alpha = (float)a.st->alpha;
@@ -983,6 +1017,7 @@ __device__ void mg_bottom_block(const MGLev& L, float* sx, float* sf, uint16_t* 
 }
 
 __global__ void __launch_bounds__(1024) k_mg_bottom(const PcgState* st, MGLev L) {
+    pdl_enter();
     if (st->done) return;
     __shared__ float sx[MG_BOTTOM_MAX];
     __shared__ float sf[MG_BOTTOM_MAX];
@@ -1021,6 +1056,7 @@ __device__ __forceinline__ unsigned cluster_size() {
 constexpr int MG_POOL_FLOATS = (MG_BOTTOM_MAX * 5 + 1) / 2;  // bottom: x, f (floats) and codes
 
 __global__ void __launch_bounds__(MG_CLUSTER_THREADS) k_mg_coarse(const PcgArgs A, const __grid_constant__ MGChain C) {
+    pdl_enter();
     if (A.st->done) return;  // the same value in every CTA of the cluster
     __shared__ float pool[MG_POOL_FLOATS];
     const long long i0 = (long long)cluster_rank() * blockDim.x + threadIdx.x;
@@ -1266,7 +1302,7 @@ static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, c
     MGLev L = mg_lev(S, l, r0, r1, z);
     const int last = (int)S.mg.size() - 1;
     if (l == last) {
-        k_mg_bottom<<<1, 1024, 0, st>>>(A.st, L);
+        launch_pdl(k_mg_bottom, 1, 1024, st, A.st, L);
         ctx->launches += 1;
         return;
     }
@@ -1280,21 +1316,23 @@ static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, c
         cfg.gridDim = dim3(S.mg_cluster);
         cfg.blockDim = dim3(MG_CLUSTER_THREADS);
         cfg.stream = st;
-        cudaLaunchAttribute at[1];
+        cudaLaunchAttribute at[2];
         at[0].id = cudaLaunchAttributeClusterDimension;
         at[0].val.clusterDim.x = S.mg_cluster;
         at[0].val.clusterDim.y = 1;
         at[0].val.clusterDim.z = 1;
+        at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[1].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = at;
-        cfg.numAttrs = 1;
+        cfg.numAttrs = 2;
         cudaLaunchKernelEx(&cfg, k_mg_coarse, A, C);
         ctx->launches += 1;
         return;
     }
     const int nb = l == 0 ? G : std::min(G, ceil_div(S.mg[l].ncell, 256));
     auto smooth = [&](int color, int first) {
-        if (l == 0) k_mg_smooth<true><<<nb, PCG_THREADS, 0, st>>>(A, L, color, first);
-        else k_mg_smooth<false><<<nb, PCG_THREADS, 0, st>>>(A, L, color, first);
+        if (l == 0) launch_pdl(k_mg_smooth<true>, nb, PCG_THREADS, st, A, L, color, first);
+        else launch_pdl(k_mg_smooth<false>, nb, PCG_THREADS, st, A, L, color, first);
     };
     for (int k = 0; k < NU; k++) {
         if (k == 0 && l == 0 && first_fused) continue;
@@ -1302,18 +1340,18 @@ static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, c
         smooth(1, 0);
         ctx->launches += 2;
     }
-    if (l == 0) k_mg_residual<true><<<nb, PCG_THREADS, 0, st>>>(A, L);
-    else k_mg_residual<false><<<nb, PCG_THREADS, 0, st>>>(A, L);
+    if (l == 0) launch_pdl(k_mg_residual<true>, nb, PCG_THREADS, st, A, L);
+    else launch_pdl(k_mg_residual<false>, nb, PCG_THREADS, st, A, L);
     MGLev Cl = mg_lev(S, l + 1, nullptr, nullptr, nullptr);
     const int nbc = std::min(G, ceil_div(S.mg[l + 1].ncell, 256));
-    k_mg_restrict<<<nbc, PCG_THREADS, 0, st>>>(A.st, L, Cl);
+    launch_pdl(k_mg_restrict, nbc, PCG_THREADS, st, A.st, L, Cl);
     mg_vcycle(ctx, A, l + 1, nullptr, nullptr, nullptr, false, -1);
-    if (l == 0) k_mg_prolong<true><<<nb, PCG_THREADS, 0, st>>>(A, L, Cl);
-    else k_mg_prolong<false><<<nb, PCG_THREADS, 0, st>>>(A, L, Cl);
+    if (l == 0) launch_pdl(k_mg_prolong<true>, nb, PCG_THREADS, st, A, L, Cl);
+    else launch_pdl(k_mg_prolong<false>, nb, PCG_THREADS, st, A, L, Cl);
     for (int k = 0; k < NU; k++) {
         smooth(1, 0);
         if (l == 0 && k == NU - 1 && dot_mode >= 0)
-            k_mg_smooth_dot<<<nb, PCG_THREADS, 0, st>>>(A, L, dot_mode);
+            launch_pdl(k_mg_smooth_dot, nb, PCG_THREADS, st, A, L, dot_mode);
         else
             smooth(0, 0);
         ctx->launches += 2;
@@ -1433,8 +1471,8 @@ static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, int prec
         if (mg) {
             const MGLev L0 = mg_lev(S, 0, nullptr, nullptr, nullptr);
             Vecs<float> vf = *reinterpret_cast<Vecs<float>*>(&v);
-            k_spmv_q<<<G, PCG_THREADS, 0, st>>>(A, vf, L0);
-            k_update_q<<<G, PCG_THREADS, 0, st>>>(A, vf, L0);
+            launch_pdl(k_spmv_q, G, PCG_THREADS, st, A, vf, L0);
+            launch_pdl(k_update_q, G, PCG_THREADS, st, A, vf, L0);
         } else {
             k_spmv<T><<<G, PCG_THREADS, 0, st>>>(A, v);
             k_update<T, 1><<<G, PCG_THREADS, 0, st>>>(A, v);
