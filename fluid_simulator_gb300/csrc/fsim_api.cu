@@ -323,9 +323,14 @@ int check_device_error(fsim_ctx* ctx) {
     return FSIM_OK;
 }
 
+// stage time between two recorded events; a pair that was not recorded reads 0
+// (and its error is cleared, so a timing query never fails a step)
 float elapsed(fsim_ctx* ctx, int a, int b) {
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev[a], ctx->ev[b]);
+    if (cudaEventElapsedTime(&ms, ctx->ev[a], ctx->ev[b]) != cudaSuccess) {
+        cudaGetLastError();
+        ms = 0.f;
+    }
     return ms;
 }
 
@@ -696,6 +701,7 @@ int fsim_step(fsim_ctx* ctx, double dt, fsim_step_stats* stats) {
     CHECK_LAUNCH(ctx);
     fsim_record(ctx, EV_PREP);
     if (P.grid_solver == FSIM_SOLVER_SOR) {
+        fsim_record(ctx, EV_PCG_SETUP);  // no setup: keeps the stage timings defined
         st.pcg_iterations = launch_sor(ctx, P.max_iters);  // BasicMacGrid returns its iteration count
         CHECK_LAUNCH(ctx);
     } else {

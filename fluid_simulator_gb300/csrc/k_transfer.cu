@@ -59,24 +59,22 @@ __device__ __forceinline__ void tent3(float f, float (&w)[3]) {
     w[2] = fmaxf(0.f, f - 0.5f);
 }
 
-// Warps come in groups of three over blocks of 32 consecutive tile+halo cells
-// (one cell per lane): the first warp of a group handles the x faces and the
-// cell-centre density of its cells, the second the y faces, the third the z
-// faces; all three walk the same particles at the same time, so the second and
-// third reads hit L1.  Each lane walks its cell's particles once and
-// accumulates, in registers, the full 2x3x3 face stencil of its axis (faces of
-// the cells at normal offset -1, 0 and transverse offsets -1, 0, +1: the union
-// of getFacesAround's 8-face stencils over the cell) and, for the x role, the
-// 3x3x3 stencil of getCellsAround -- the merged contribution of all particles
-// of the cell.  The next particle's index and data are fetched while the
-// current one is accumulated.  The lane then adds the entries inside the tile
-// to the tile's shared accumulators (lanes hold distinct cells, so a warp's
-// adds never collide).
+// Warps come in pairs over blocks of 32 consecutive tile+halo cells (one cell
+// per lane).  The even warp of a pair handles the x faces and the cell-centre
+// density of its cells, the odd warp the y and z faces; both walk the same
+// particles at the same time, so the second reads hit L1.  Each lane walks its
+// cell's particles once and accumulates, in registers, the full 2x3x3 face
+// stencil of its axes (faces of the cells at normal offset -1, 0 and
+// transverse offsets -1, 0, +1: the union of getFacesAround's 8-face stencils
+// over the cell) and the 3x3x3 stencil of getCellsAround -- the merged
+// contribution of all particles of the cell.  It then adds the entries inside
+// the tile to the tile's shared accumulators (lanes hold distinct cells, so a
+// warp's adds never collide).
 constexpr int P2G_THREADS_V2 = 384;
 
-// accumulators of one lane: [0,18) weights, [18,36) values of the role's axis;
-// the x role adds [36,63) density
-constexpr int NACC = 63;
+// accumulators of one lane: role 0 uses [0,18) weights x, [18,36) values x,
+// [36,63) density; role 1 uses [0,18)/[18,36) for y and [36,54)/[54,72) for z
+constexpr int NACC = 72;
 
 template <bool APIC, int AX, int OW, int OV>
 __device__ __forceinline__ void p2g_face_axis(const float (&f)[3], const float (&wt)[3][3], float va,
@@ -139,15 +137,11 @@ __global__ void __launch_bounds__(P2G_THREADS_V2, 1) k_p2g(const P2GArgs a) {
     __syncthreads();
     const float hinv = a.g.hinv, h = a.g.h;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int role = warp % 3;                  // face axis; role 0 also the density
-    const int groups = P2G_THREADS_V2 / 96;     // warp groups per CTA
+    const int role = warp & 1;                  // 0: x faces + density, 1: y and z faces
+    const int pairs = P2G_THREADS_V2 / 64;      // warp pairs per CTA
     constexpr int HC = QX * QY * QZ;
-    const float* pv = a.p.v[role];
-    const float* c0p = a.p.c[3 * role];
-    const float* c1p = a.p.c[3 * role + 1];
-    const float* c2p = a.p.c[3 * role + 2];
 
-    for (int blk = warp / 3; blk * 32 < HC; blk += groups) {
+    for (int blk = warp >> 1; blk * 32 < HC; blk += pairs) {
         const int hc = blk * 32 + lane;
         if (hc >= HC) continue;
         const int hz = hc % QZ, hy = (hc / QZ) % QY, hx = hc / (QZ * QY);
@@ -161,37 +155,21 @@ __global__ void __launch_bounds__(P2G_THREADS_V2, 1) k_p2g(const P2GArgs a) {
 #pragma unroll
         for (int e = 0; e < NACC; e++) acc[e] = 0.f;
 
-        // particle k's fields, fetched one particle ahead
-        uint32_t i = a.perm[beg];
-        float np[3], nv, nc[3];
-        np[0] = a.p.p[0][i];
-        np[1] = a.p.p[1][i];
-        np[2] = a.p.p[2][i];
-        nv = pv[i];
-        nc[0] = APIC ? c0p[i] : 0.f;
-        nc[1] = APIC ? c1p[i] : 0.f;
-        nc[2] = APIC ? c2p[i] : 0.f;
         for (int k = beg; k < end; k++) {
-            const float px = np[0], py = np[1], pz = np[2], va = nv;
-            const float cm[3] = {nc[0], nc[1], nc[2]};
-            if (k + 1 < end) {
-                const uint32_t in = a.perm[k + 1];
-                np[0] = a.p.p[0][in];
-                np[1] = a.p.p[1][in];
-                np[2] = a.p.p[2][in];
-                nv = pv[in];
-                if (APIC) {
-                    nc[0] = c0p[in];
-                    nc[1] = c1p[in];
-                    nc[2] = c2p[in];
-                }
-            }
-            float f[3] = {px * hinv - (float)cc[0], py * hinv - (float)cc[1], pz * hinv - (float)cc[2]};
+            const uint32_t i = a.perm[k];
+            float f[3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) f[d] = a.p.p[d][i] * hinv - (float)cc[d];
             float wt[3][3];
 #pragma unroll
             for (int d = 0; d < 3; d++) tent3(f[d], wt[d]);
             if (role == 0) {
-                p2g_face_axis<APIC, 0, 0, 18>(f, wt, va, cm, h, acc);
+                float cm[3] = {0.f, 0.f, 0.f};
+                if (APIC) {
+#pragma unroll
+                    for (int q = 0; q < 3; q++) cm[q] = a.p.c[q][i];
+                }
+                p2g_face_axis<APIC, 0, 0, 18>(f, wt, a.p.v[0][i], cm, h, acc);
 #pragma unroll
                 for (int ox = 0; ox < 3; ox++)
 #pragma unroll
@@ -200,10 +178,17 @@ __global__ void __launch_bounds__(P2G_THREADS_V2, 1) k_p2g(const P2GArgs a) {
 #pragma unroll
                         for (int oz = 0; oz < 3; oz++) acc[36 + (ox * 3 + oy) * 3 + oz] += wxy * wt[2][oz];
                     }
-            } else if (role == 1) {
-                p2g_face_axis<APIC, 1, 0, 18>(f, wt, va, cm, h, acc);
             } else {
-                p2g_face_axis<APIC, 2, 0, 18>(f, wt, va, cm, h, acc);
+                float cmy[3] = {0.f, 0.f, 0.f}, cmz[3] = {0.f, 0.f, 0.f};
+                if (APIC) {
+#pragma unroll
+                    for (int q = 0; q < 3; q++) {
+                        cmy[q] = a.p.c[3 + q][i];
+                        cmz[q] = a.p.c[6 + q][i];
+                    }
+                }
+                p2g_face_axis<APIC, 1, 0, 18>(f, wt, a.p.v[1][i], cmy, h, acc);
+                p2g_face_axis<APIC, 2, 36, 54>(f, wt, a.p.v[2][i], cmz, h, acc);
             }
         }
         if (role == 0) {
@@ -215,10 +200,9 @@ __global__ void __launch_bounds__(P2G_THREADS_V2, 1) k_p2g(const P2GArgs a) {
                 if (lx < 0 || ly < 0 || lz < 0 || lx >= PX || ly >= PY || lz >= PZ) continue;
                 atomicAdd(&s_avg[(lx * PY + ly) * PZ + lz], acc[36 + e]);
             }
-        } else if (role == 1) {
-            p2g_flush_axis<1, 0, 18>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
         } else {
-            p2g_flush_axis<2, 0, 18>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
+            p2g_flush_axis<1, 0, 18>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
+            p2g_flush_axis<2, 36, 54>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
         }
     }
     __syncthreads();
