@@ -224,6 +224,30 @@ int run_keys(fsim_ctx* ctx, int do_advect, int do_push, int do_stop, double dt) 
     return sort_by_cell(ctx);
 }
 
+// HashedParticles::pushParticlesApart (hashedParticles.cpp:64-107), Jacobi
+// semantics (k_push_apart); needs the cell sort of the current positions
+int push_apart_pass(fsim_ctx* ctx) {
+    const GridGeom& g = ctx->g;
+    const double pr = ctx->prm.particle_r;
+    if (2.0 * pr > g.hd)
+        return set_error(ctx, FSIM_E_UNSUPPORTED, "push-apart needs particle_r <= h/2 (neighbours within one cell)");
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; k++) {
+        const double low = g.hd + pr * 1.01;  // particleLow (hashedParticles.cpp:67)
+        lo[k] = (float)low;
+        hi[k] = (float)(g.dims[k] - low);
+    }
+    float* tmp[3] = {ctx->buf[1 - ctx->cur].p[0], ctx->buf[1 - ctx->cur].p[1], ctx->buf[1 - ctx->cur].p[2]};
+    launch_push_apart(ctx->buf[ctx->cur], ctx->perm, ctx->cstart, g, ctx->n, pr, lo, hi, tmp, ctx->stream);
+    ctx->launches += ctx->n > 0 ? 1 : 0;
+    CHECK_LAUNCH(ctx);
+    for (int k = 0; k < 3; k++)
+        FSIM_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->buf[ctx->cur].p[k], tmp[k], (size_t)ctx->n * sizeof(float),
+                                           cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->sorted = false;
+    return FSIM_OK;
+}
+
 int run_particle_only(fsim_ctx* ctx, int do_advect, int do_push, int do_stop, double dt) {
     AdvectArgs a;
     fill_advect_args(ctx, a, dt);
@@ -336,7 +360,6 @@ float elapsed(fsim_ctx* ctx, int a, int b) {
 
 int validate_params(const fsim_params* p, std::string& why) {
     if (p->transfer < FSIM_PIC || p->transfer > FSIM_APIC) { why = "transfer type"; return FSIM_E_INVALID; }
-    if (p->push_apart_enabled) { why = "push-apart is not built"; return FSIM_E_UNSUPPORTED; }
     if (p->max_iters < 0) { why = "max_iters"; return FSIM_E_INVALID; }
     if (!(p->fluid_density > 0)) { why = "fluid_density"; return FSIM_E_INVALID; }
     if (p->precision < FSIM_PREC_MIXED || p->precision > FSIM_PREC_FP64) { why = "precision"; return FSIM_E_INVALID; }
@@ -620,7 +643,11 @@ int fsim_stage(fsim_ctx* ctx, int stage, double dt, fsim_step_stats* stats) {
             ctx->n = ctx->h_misc[0];
             ctx->sorted = false;
             break;
-        case FSIM_STAGE_PUSH_APART: return set_error(ctx, FSIM_E_UNSUPPORTED, "push-apart is not built");
+        case FSIM_STAGE_PUSH_APART:
+            // sort the current positions (no movement), then one push-apart pass
+            if ((rc = run_keys(ctx, 0, 0, 0, dt))) return rc;
+            rc = push_apart_pass(ctx);
+            break;
         case FSIM_STAGE_PUSH_OUT: rc = run_particle_only(ctx, 0, 1, 0, dt); break;
         case FSIM_STAGE_STOP: rc = run_particle_only(ctx, 0, 0, 1, dt); break;
         case FSIM_STAGE_P2G:
@@ -678,7 +705,31 @@ int fsim_step(fsim_ctx* ctx, double dt, fsim_step_stats* stats) {
     fsim_record(ctx, EV_START);
     if (P.spawning_enabled && (rc = do_spawn(ctx, dt))) return rc;
     // advect + push-out + stop + keys, then the counting sort
-    {
+    if (P.push_apart_enabled) {
+        // advect (+ sinks) with keys and a sort, push apart, then push-out /
+        // stop with keys (deleted particles stay deleted) and the step's sort
+        AdvectArgs a;
+        fill_advect_args(ctx, a, dt);
+        a.do_advect = 1;
+        a.do_key = 1;
+        FSIM_CUDA_TRY(ctx, cudaMemsetAsync(ctx->count, 0, (size_t)ctx->g.ncell * sizeof(int), ctx->stream));
+        launch_advect(a, ctx->stream);
+        ctx->launches += ctx->n > 0 ? 1 : 0;
+        CHECK_LAUNCH(ctx);
+        fsim_record(ctx, EV_ADVECT);
+        if ((rc = sort_by_cell(ctx))) return rc;
+        if ((rc = push_apart_pass(ctx))) return rc;
+        fsim_record(ctx, EV_APART);
+        fill_advect_args(ctx, a, dt);
+        a.do_push = 1;
+        a.do_stop = P.stop_particles;
+        a.do_key = 1;
+        a.keep_dead = 1;
+        FSIM_CUDA_TRY(ctx, cudaMemsetAsync(ctx->count, 0, (size_t)ctx->g.ncell * sizeof(int), ctx->stream));
+        launch_advect(a, ctx->stream);
+        ctx->launches += ctx->n > 0 ? 1 : 0;
+        CHECK_LAUNCH(ctx);
+    } else {
         AdvectArgs a;
         fill_advect_args(ctx, a, dt);
         a.do_advect = 1;
@@ -689,8 +740,8 @@ int fsim_step(fsim_ctx* ctx, double dt, fsim_step_stats* stats) {
         launch_advect(a, ctx->stream);
         ctx->launches += ctx->n > 0 ? 1 : 0;
         CHECK_LAUNCH(ctx);
+        fsim_record(ctx, EV_ADVECT);
     }
-    fsim_record(ctx, EV_ADVECT);
     if ((rc = sort_by_cell(ctx))) return rc;
     fsim_record(ctx, EV_SORT);
     launch_p2g(ctx);
@@ -726,7 +777,8 @@ int fsim_step(fsim_ctx* ctx, double dt, fsim_step_stats* stats) {
         st.kernel_launches = (int)(ctx->launches - launches0);
         if (P.timing) {
             st.ms_simulate_particles = elapsed(ctx, EV_START, EV_ADVECT);
-            st.ms_p2g = elapsed(ctx, EV_ADVECT, EV_P2G);
+            st.ms_push_apart = P.push_apart_enabled ? elapsed(ctx, EV_ADVECT, EV_APART) : 0.f;
+            st.ms_p2g = elapsed(ctx, P.push_apart_enabled ? EV_APART : EV_ADVECT, EV_P2G);
             st.ms_p2g_kernel = elapsed(ctx, EV_SORT, EV_P2G);
             st.ms_prep = elapsed(ctx, EV_P2G, EV_PREP);
             st.ms_pcg_setup = elapsed(ctx, EV_PREP, EV_PCG_SETUP);

@@ -129,6 +129,7 @@ struct AdvectArgs {
     ParticleBuf p;
     long long n;
     int do_advect, do_push, do_stop, do_key, despawn;
+    int keep_dead;         // particles whose key is already DEAD stay dead (second pass of a step)
     float dt;
     float lo[3], hi[3];    // advection clamp band (gridLow / gridHigh)
     float plo[3], phi[3];  // push-out clamp band
@@ -152,6 +153,8 @@ void launch_spawn_sphere(ParticleBuf p, long long first, int count, const fsim_o
 void launch_spawn_disc(ParticleBuf p, long long first, int ncells, const fsim_obstacle& o,
                        const GridGeom& g, int cy, const int* cells_xz, uint64_t seed,
                        uint32_t first_id, bool ids, cudaStream_t s);
+void launch_push_apart(ParticleBuf p, const uint32_t* perm, const int* cstart, const GridGeom& g, long long n,
+                       double r, const float lo[3], const float hi[3], float* const out[3], cudaStream_t s);
 void launch_gfx(ParticleBuf p, long long n, const float* avg, const GridGeom& g,
                 fsim_particle_gfx* out, cudaStream_t s);
 
@@ -186,7 +189,7 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
 // Event slots of a step (recorded when fsim_params.timing is set).
 enum {
     EV_START = 0, EV_ADVECT, EV_SORT, EV_P2G, EV_PREP, EV_PCG_SETUP, EV_SOLVE, EV_EXTRAP, EV_G2P, EV_GUESS0,
-    EV_GUESS1, EV_COUNT
+    EV_GUESS1, EV_APART, EV_COUNT
 };
 inline void fsim_record(fsim_ctx* ctx, int k) {
     if (ctx->prm.timing) cudaEventRecord(ctx->ev[k], ctx->stream);

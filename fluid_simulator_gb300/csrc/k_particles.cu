@@ -34,8 +34,8 @@ __global__ void __launch_bounds__(256) k_advect(const AdvectArgs a) {
     if (live) {
         float px = a.p.p[0][i], py = a.p.p[1][i], pz = a.p.p[2][i];
         float vx = a.p.v[0][i], vy = a.p.v[1][i], vz = a.p.v[2][i];
-        bool dead = false;
-        if (a.do_advect) {
+        bool dead = a.keep_dead && a.key[i] == FSIM_DEAD_KEY;
+        if (a.do_advect && !dead) {
             const float dt = a.dt, pr = a.pr;
             float t = 0.f;
             int run = 0;
@@ -192,7 +192,9 @@ __global__ void __launch_bounds__(256) k_advect(const AdvectArgs a) {
             }
         }
         if (a.do_stop) { vx = 0.f; vy = 0.f; vz = 0.f; }
-        if (a.do_advect || a.do_push) {
+        if (dead && a.keep_dead) {
+            // deleted by the first pass: nothing moves
+        } else if (a.do_advect || a.do_push) {
             a.p.p[0][i] = px; a.p.p[1][i] = py; a.p.p[2][i] = pz;
         }
         if (a.do_advect || a.do_stop) {
@@ -303,6 +305,55 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_tile_scan(const int* in, long 
         e += v[k];
     }
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[n] = e;
+}
+
+// HashedParticles::pushParticlesApart (hashedParticles.cpp:64-107) with
+// deterministic (Jacobi) semantics: every particle moves by the sum, over all
+// other particles within distance 2r (and not closer than 1e-4), of half the
+// overlap along their separation, computed from the positions at the start of
+// the pass, then is clamped to [h + 1.01 r, dims - h - 1.01 r].  (The
+// reference updates both particles of a pair in place, in a racy parallel
+// loop; for an isolated pair both give the same result.)  Neighbours come from
+// the cell sort: with 2r <= h they lie in the 27 cells around the particle's
+// cell.  New positions go to out; thread = sorted slot.
+__global__ void k_push_apart(ParticleBuf p, const uint32_t* perm, const int* cstart, GridGeom g, long long n,
+                             float r, float lo0, float lo1, float lo2, float hi0, float hi1, float hi2,
+                             float* out0, float* out1, float* out2) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long live = cstart[g.ncell];
+    if (k >= live || k >= n) return;
+    const uint32_t i = perm[k];
+    const float xi = p.p[0][i], yi = p.p[1][i], zi = p.p[2][i];
+    const int cx = (int)(xi * g.hinv), cy = (int)(yi * g.hinv), cz = (int)(zi * g.hinv);
+    const float D = 2.f * r, D2 = D * D;
+    float dx = 0.f, dy = 0.f, dz = 0.f;
+    for (int ox = -1; ox <= 1; ox++) {
+        const int x = cx + ox;
+        if (x < 0 || x >= g.nx) continue;
+        for (int oy = -1; oy <= 1; oy++) {
+            const int y = cy + oy;
+            if (y < 0 || y >= g.ny) continue;
+            // the three z cells of a row are one contiguous run of the sort
+            const int zb = max(cz - 1, 0), ze = min(cz + 2, g.nz);
+            const long long row = gidx(g, x, y, 0);
+            const int b = cstart[row + zb], e = cstart[row + ze];
+            for (int q = b; q < e; q++) {
+                const uint32_t j = perm[q];
+                if (j == i) continue;
+                const float px = xi - p.p[0][j], py = yi - p.p[1][j], pz = zi - p.p[2][j];
+                const float d2 = px * px + py * py + pz * pz;
+                if (d2 > D2 || d2 < 1e-8f) continue;
+                const float d = sqrtf(d2);
+                const float t = (D - d) / d * 0.5f;
+                dx += px * t;
+                dy += py * t;
+                dz += pz * t;
+            }
+        }
+    }
+    out0[i] = fminf(fmaxf(xi + dx, lo0), hi0);
+    out1[i] = fminf(fmaxf(yi + dy, lo1), hi1);
+    out2[i] = fminf(fmaxf(zi + dz, lo2), hi2);
 }
 
 __global__ void k_scatter(const uint32_t* key, const uint32_t* rank, const int* cstart, uint32_t* perm,
@@ -417,6 +468,13 @@ void launch_scan(const int* in, int* out, long long n, int* block_sums, cudaStre
     k_tile_sums<<<nt, SCAN_THREADS, 0, s>>>(in, n, block_sums);
     k_scan_sums<<<1, SCAN_THREADS, 0, s>>>(block_sums, nt);
     k_tile_scan<<<nt, SCAN_THREADS, 0, s>>>(in, n, block_sums, out);
+}
+
+void launch_push_apart(ParticleBuf p, const uint32_t* perm, const int* cstart, const GridGeom& g, long long n,
+                       double r, const float lo[3], const float hi[3], float* const out[3], cudaStream_t s) {
+    if (n <= 0) return;
+    k_push_apart<<<ceil_div(n, 256), 256, 0, s>>>(p, perm, cstart, g, n, (float)r, lo[0], lo[1], lo[2], hi[0], hi[1],
+                                                  hi[2], out[0], out[1], out[2]);
 }
 
 void launch_scatter(const uint32_t* key, const uint32_t* rank, const int* cstart, uint32_t* perm,

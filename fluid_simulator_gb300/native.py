@@ -166,14 +166,14 @@ def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: 
                    pressure_enabled: bool = False, pressure_k: float = 2.0, average_pressure: float = 2.0,
                    fluid_density: float = 1.0, timing: bool = False, precond: int = PRECOND_MG,
                    mg_sweeps: int = 0, mg_coarse_sweeps: int = 0, mg_cluster_sweeps: int = 0,
-                   grid_solver: int = SOLVER_PCG) -> Params:
+                   grid_solver: int = SOLVER_PCG, push_apart: bool = False) -> Params:
     """Parameters of the dam-break workloads (reference parameter names in fsim.h)."""
     p = Params()
     p.transfer = transfer
     p.flip_ratio = flip_ratio
     p.gravity = gravity
     p.gravity_enabled = int(gravity_enabled)
-    p.push_apart_enabled = 0
+    p.push_apart_enabled = int(push_apart)
     p.spawning_enabled = int(spawning)
     p.despawning_enabled = int(despawning)
     p.stop_particles = int(stop_particles)

@@ -102,7 +102,8 @@ enum fsim_warm_start {
 enum fsim_stage {
     FSIM_STAGE_SPAWN = 0,
     FSIM_STAGE_ADVECT = 1,
-    FSIM_STAGE_PUSH_APART = 2, /* not built: returns FSIM_E_UNSUPPORTED */
+    FSIM_STAGE_PUSH_APART = 2, /* HashedParticles::pushParticlesApart (hashedParticles.cpp:64-107) with
+                                  deterministic Jacobi semantics (see push_apart_enabled) */
     FSIM_STAGE_PUSH_OUT = 3,
     FSIM_STAGE_STOP = 4,
     FSIM_STAGE_P2G = 5,       /* sort by cell + resetGridValues + p2gTransfer + marking */
@@ -143,7 +144,11 @@ typedef struct fsim_params {
     float flip_ratio;
     float gravity;          /* signed, added to v_y * dt */
     int gravity_enabled;
-    int push_apart_enabled; /* must be 0 (not built) */
+    int push_apart_enabled; /* SimulatorConfig::pushApartEnabled: after advection every particle
+                               moves by the sum of half-overlaps with all particles within 2r
+                               (positions from before the pass), then is clamped; the reference's
+                               in-place pairwise update is racy, this is its deterministic form.
+                               Needs particle_r <= h/2. */
     int spawning_enabled;
     int despawning_enabled;
     int stop_particles;

@@ -22,8 +22,9 @@
 //
 // Parts of the reference interface that only the reference's own Simulator
 // uses internally (face/cell stencil helpers, grid reset, P2G helpers, the
-// intersection hash) are not declared; pushParticlesApart throws, as the GPU
-// library does not build it.  BasicMacGrid selects the library's SOR solver.  Default particle positions of HashedParticles
+// intersection hash) are not declared.  Push-apart runs with the library's
+// deterministic (Jacobi) semantics.  BasicMacGrid selects the library's SOR
+// solver.  Default particle positions of HashedParticles
 // use a SplitMix64 generator instead of std::rand.
 //
 // Requires glm (glm::dvec3, glm::ivec3) and C++17.
@@ -237,8 +238,14 @@ public:
         particles.resize(w);
     }
 
+    // Reference: hashedParticles.cpp:64-107; the library's deterministic (Jacobi)
+    // push-apart pass on the bound context (FSIM_STAGE_PUSH_APART)
     void pushParticlesApart(bool /*parallel*/) {
-        throw std::runtime_error("pushParticlesApart is not built on the GPU path");
+        if (!device) throw std::runtime_error("pushParticlesApart: the particles are not bound to a Simulator");
+        if (edited) push(device);
+        facade_detail::check(fsim_stage(device, FSIM_STAGE_PUSH_APART, 0.0, nullptr), device,
+                             "fsim_stage(PUSH_APART)");
+        host_valid = false;
     }
 
     const double z;
@@ -590,7 +597,7 @@ private:
         p.flip_ratio = config.flipRatio;
         p.gravity = config.gravity;
         p.gravity_enabled = config.gravityEnabled;
-        p.push_apart_enabled = 0;  // not built on the GPU path
+        p.push_apart_enabled = config.pushApartEnabled;
         p.spawning_enabled = config.particleSpawningEnabled;
         p.despawning_enabled = config.particleDespawningEnabled;
         p.stop_particles = config.stopParticles;

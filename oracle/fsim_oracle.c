@@ -496,6 +496,75 @@ static inline double clampd(double v, double lo, double hi) { return v < lo ? lo
 
 /* Simulator::pushParticlesOutOfObstacles (simulator.cpp:253-312);
  * MacGrid::getMinMaxRect (macGrid.h:139-145). */
+/* HashedParticles::pushParticlesApart (hashedParticles.cpp:64-107) with the
+ * GPU library's deterministic (Jacobi) semantics: from the positions at the
+ * start of the pass, every particle moves by the sum over all others within
+ * 2r (and at least 1e-4 away) of half the overlap along their separation, then
+ * is clamped to [h + 1.01 r, dims - h - 1.01 r].  The reference moves both
+ * particles of a pair in place in a racy parallel loop, so it has no single
+ * result to restate; for an isolated pair both agree.  O(n) with a cell hash of
+ * edge h (neighbours within 2r <= h are in the 27 surrounding cells). */
+static void stage_push_apart(sim *s) {
+    const int n = s->n;
+    if (n <= 0) return;
+    const double r = s->p.particle_r, D = 2.0 * r, D2 = D * D;
+    const double lo[3] = {s->cd.x + r * 1.01, s->cd.y + r * 1.01, s->cd.z + r * 1.01};
+    const double hi[3] = {s->dims.x - lo[0], s->dims.y - lo[1], s->dims.z - lo[2]};
+    int *cnt = (int *)calloc((size_t)s->ncell + 1, sizeof(int));
+    int *idx = (int *)malloc((size_t)n * sizeof(int));
+    int *key = (int *)malloc((size_t)n * sizeof(int));
+    for (int i = 0; i < n; i++) {
+        int cx = (int)(s->pt[i].pos.x * s->cdi.x), cy = (int)(s->pt[i].pos.y * s->cdi.y),
+            cz = (int)(s->pt[i].pos.z * s->cdi.z);
+        cx = cx < 0 ? 0 : (cx >= s->nx ? s->nx - 1 : cx);
+        cy = cy < 0 ? 0 : (cy >= s->ny ? s->ny - 1 : cy);
+        cz = cz < 0 ? 0 : (cz >= s->nz ? s->nz - 1 : cz);
+        key[i] = cx * s->yz + cy * s->nz + cz;
+        cnt[key[i] + 1]++;
+    }
+    for (int c = 0; c < s->ncell; c++) cnt[c + 1] += cnt[c];
+    int *fill = (int *)malloc((size_t)s->ncell * sizeof(int));
+    memcpy(fill, cnt, (size_t)s->ncell * sizeof(int));
+    for (int i = 0; i < n; i++) idx[fill[key[i]]++] = i;
+    d3 *np = (d3 *)malloc((size_t)n * sizeof(d3));
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++) {
+        const d3 pi = s->pt[i].pos;
+        const int c = key[i], cx = c / s->yz, cy = (c / s->nz) % s->ny, cz = c % s->nz;
+        double dx = 0.0, dy = 0.0, dz = 0.0;
+        for (int x = cx - 1; x <= cx + 1; x++)
+            for (int y = cy - 1; y <= cy + 1; y++)
+                for (int z = cz - 1; z <= cz + 1; z++) {
+                    if (x < 0 || y < 0 || z < 0 || x >= s->nx || y >= s->ny || z >= s->nz) continue;
+                    const int cc = x * s->yz + y * s->nz + z;
+                    for (int q = cnt[cc]; q < cnt[cc + 1]; q++) {
+                        const int j = idx[q];
+                        if (j == i) continue;
+                        const double px = pi.x - s->pt[j].pos.x, py = pi.y - s->pt[j].pos.y,
+                                     pz = pi.z - s->pt[j].pos.z;
+                        const double d2 = px * px + py * py + pz * pz;
+                        if (d2 > D2 || d2 < 1e-8) continue;
+                        const double d = sqrt(d2);
+                        const double t = (D - d) / d * 0.5;
+                        dx += px * t;
+                        dy += py * t;
+                        dz += pz * t;
+                    }
+                }
+        d3 q = {pi.x + dx, pi.y + dy, pi.z + dz};
+        q.x = q.x < lo[0] ? lo[0] : (q.x > hi[0] ? hi[0] : q.x);
+        q.y = q.y < lo[1] ? lo[1] : (q.y > hi[1] ? hi[1] : q.y);
+        q.z = q.z < lo[2] ? lo[2] : (q.z > hi[2] ? hi[2] : q.z);
+        np[i] = q;
+    }
+    for (int i = 0; i < n; i++) s->pt[i].pos = np[i];
+    free(np);
+    free(fill);
+    free(key);
+    free(idx);
+    free(cnt);
+}
+
 static void stage_push_out(sim *s) {
     const double pr = s->p.particle_r;
     d3 lo = {s->cd.x + pr * 1.01, s->cd.y + pr * 1.01, s->cd.z + pr * 1.01};
@@ -1041,7 +1110,7 @@ int oracle_stage(void *h, int stage, double dt) {
     switch (stage) {
         case ORACLE_STAGE_SPAWN: stage_spawn(s, dt); return 0;
         case ORACLE_STAGE_ADVECT: stage_advect(s, dt); return 0;
-        case ORACLE_STAGE_PUSH_APART: return -1; /* disabled in every workload; not restated */
+        case ORACLE_STAGE_PUSH_APART: stage_push_apart(s); return 0;
         case ORACLE_STAGE_PUSH_OUT: stage_push_out(s); return 0;
         case ORACLE_STAGE_STOP:
             for (int i = 0; i < s->n; i++) { s->pt[i].v.x = 0; s->pt[i].v.y = 0; s->pt[i].v.z = 0; }
@@ -1065,6 +1134,7 @@ int oracle_step(void *h, double dt) {
     sim *s = (sim *)h;
     if (s->p.spawning_enabled) stage_spawn(s, dt);
     stage_advect(s, dt);
+    if (s->p.push_apart_enabled) stage_push_apart(s);
     stage_push_out(s);
     if (s->p.stop_particles) oracle_stage(s, ORACLE_STAGE_STOP, dt);
     stage_p2g(s);

@@ -139,7 +139,8 @@ def make_params(resolution: float, *, transfer: int = FLIP, flip_ratio: float = 
                 gravity_enabled: bool = True, spawning: bool = False, despawning: bool = False,
                 stop_particles: bool = False, pressure_enabled: bool = False,
                 pressure_k: float = 2.0, average_pressure: float = 2.0,
-                fluid_density: float = 1.0, two_d: bool = False, grid_solver: int = 0) -> OracleParams:
+                fluid_density: float = 1.0, two_d: bool = False, grid_solver: int = 0,
+                push_apart: bool = False) -> OracleParams:
     p = OracleParams()
     p.resolution = resolution
     p.dims[:] = list(dims)
@@ -149,7 +150,7 @@ def make_params(resolution: float, *, transfer: int = FLIP, flip_ratio: float = 
     p.flip_ratio = flip_ratio
     p.gravity = gravity
     p.gravity_enabled = int(gravity_enabled)
-    p.push_apart_enabled = 0
+    p.push_apart_enabled = int(push_apart)
     p.spawning_enabled = int(spawning)
     p.despawning_enabled = int(despawning)
     p.stop_particles = int(stop_particles)

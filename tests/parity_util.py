@@ -34,7 +34,8 @@ def make_pair(pos, resolution, transfer, *, vel=None, c=None, lib="port", thread
     g = N.Simulation(resolution, p, track_ids=True)
     g.set_particles(pos, vel, None if c is None else np.asarray(c, np.float32).reshape(-1, 9))
     okw = {k: v for k, v in kw.items() if k in ("spawning", "despawning", "stop_particles", "gravity",
-                                                "flip_ratio", "top_solid", "pressure_enabled", "grid_solver")}
+                                                "flip_ratio", "top_solid", "pressure_enabled", "grid_solver",
+                                                "push_apart")}
     op = O.make_params(resolution, transfer=TRANSFER_O[transfer], tol=tol, max_iters=max_iters, **okw)
     o = O.Oracle(op, pos.astype(np.float64),
                  None if vel is None else np.asarray(vel, np.float32).astype(np.float64),

@@ -108,6 +108,38 @@ def test_sor_matches_oracle(gpu, port_lib, pressure_enabled):
         assert_close_field(g.grid(fg), o.grid(fo), 1e-4, f"v2 after SOR {fg}")
 
 
+def test_push_apart_matches_oracle(gpu, port_lib):
+    """One push-apart pass (Jacobi semantics) from identical, overlapping particles."""
+    pos, vel, c = moving_state(32, N.FLIP)
+    g, o = make_pair(pos, 32, N.FLIP, vel=vel, threads=4, push_apart=True)
+    before = g.particles()[0]
+    g.stage(N.STAGE_PUSH_APART, DT32)
+    o.stage(O.STAGE_PUSH_APART, DT32)
+    gp = g.particles()[0]
+    op = o.particles()[0]
+    moved = np.abs(gp - before).max(axis=1) > 0
+    assert moved.mean() > 0.1  # the scene has overlapping pairs
+    assert np.abs(gp - op).max() <= 2e-6
+
+
+@pytest.mark.parametrize("transfer", [N.FLIP, N.APIC])
+def test_full_step_with_push_apart(gpu, port_lib, transfer):
+    """Whole steps with push-apart on both sides, one-step-error protocol."""
+    pos = dam_break(GridSpec(32), seed=2)
+    g, o = make_pair(pos, 32, transfer, threads=4, tol=1e-9, gpu_tol=1e-9, max_iters=1000, push_apart=True)
+    for s in range(4):
+        sync_oracle_particles_from_gpu(g, o)
+        g.step(DT32)
+        o.step(DT32)
+        gp, gv, _ = g.particles()
+        op, ov, _ = o.particles()
+        assert gp.shape == op.shape
+        dv = np.abs(gv - ov).max() / max(1e-6, np.abs(ov).max())
+        dp = np.abs(gp - op).max() / g.h
+        assert dp < 1e-3, f"step {s}: position error {dp} cells"
+        assert dv < 1e-3, f"step {s}: velocity error {dv}"
+
+
 def test_multigrid_needs_far_fewer_iterations(gpu, port_lib):
     """Both preconditioners reach the same pressure; multigrid in far fewer iterations."""
     pos, vel, c = moving_state(32, N.FLIP)
