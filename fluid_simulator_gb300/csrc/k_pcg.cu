@@ -1037,7 +1037,173 @@ constexpr long long MG_CLUSTER_CELLS = 300000;  // largest level handed to the c
 struct MGChain {
     MGLev lev[MG_MAX_LEVELS];
     int lc, last, nu;
+    int ls;  // first level small enough to run in one CTA's shared memory (<= last)
 };
+
+// ---- the smallest levels in one CTA's shared memory ----------------------------
+// Levels with at most MG_SMEM_CELLS cells are copied (dense, z fastest) into
+// shared memory and run their part of the V-cycle there: the same red-black
+// Gauss-Seidel, full-weighting restriction (x 0.5) and trilinear prolongation
+// as the global kernels, with __syncthreads between passes instead of cluster
+// barriers and global-memory round trips.
+constexpr int MG_SMEM_CELLS = 4096;
+
+struct SLev {
+    int nx, ny, nz, n;
+    float *x, *f, *r;
+    uint16_t* code;
+};
+
+__device__ __forceinline__ int sidx(const SLev& L, int x, int y, int z) { return (x * L.ny + y) * L.nz + z; }
+
+__device__ void s_smooth(const SLev& L, int color) {
+    for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
+        const int z = i % L.nz, y = (i / L.nz) % L.ny, x = i / (L.nz * L.ny);
+        if (((x + y + z) & 1) != color) continue;
+        const uint16_t cc = L.code[i];
+        if (!(cc & CODE_FLUID)) continue;
+        float s = 0.f;
+        if (cc & 1) s += L.x[i + L.ny * L.nz];
+        if (cc & 2) s += L.x[i - L.ny * L.nz];
+        if (cc & 4) s += L.x[i + L.nz];
+        if (cc & 8) s += L.x[i - L.nz];
+        if (cc & 16) s += L.x[i + 1];
+        if (cc & 32) s += L.x[i - 1];
+        L.x[i] = (L.f[i] + s) * c_rcp[code_ns(cc)];
+    }
+    __syncthreads();
+}
+
+__device__ void s_residual(const SLev& L) {
+    for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
+        const uint16_t cc = L.code[i];
+        float rv = 0.f;
+        if (cc & CODE_FLUID) {
+            float s = 0.f;
+            if (cc & 1) s += L.x[i + L.ny * L.nz];
+            if (cc & 2) s += L.x[i - L.ny * L.nz];
+            if (cc & 4) s += L.x[i + L.nz];
+            if (cc & 8) s += L.x[i - L.nz];
+            if (cc & 16) s += L.x[i + 1];
+            if (cc & 32) s += L.x[i - 1];
+            rv = L.f[i] - ((float)code_ns(cc) * L.x[i] - s);
+        }
+        L.r[i] = rv;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ float fw_weight(int d) { return (d == 0 || d == 1) ? 0.75f : 0.25f; }
+
+// coarse f = 0.5 * sum_fine P r (fine fluid only), coarse x = 0
+__device__ void s_restrict(const SLev& F, const SLev& C) {
+    for (int i = threadIdx.x; i < C.n; i += blockDim.x) {
+        const int cz = i % C.nz, cy = (i / C.nz) % C.ny, cx = i / (C.nz * C.ny);
+        C.x[i] = 0.f;
+        if (!(C.code[i] & CODE_FLUID)) {
+            C.f[i] = 0.f;
+            continue;
+        }
+        float sum = 0.f;
+        for (int dx = -1; dx <= 2; dx++) {
+            const int fx = 2 * cx + dx;
+            if (fx < 0 || fx >= F.nx) continue;
+            for (int dy = -1; dy <= 2; dy++) {
+                const int fy = 2 * cy + dy;
+                if (fy < 0 || fy >= F.ny) continue;
+                const float wxy = fw_weight(dx) * fw_weight(dy);
+                for (int dz = -1; dz <= 2; dz++) {
+                    const int fz = 2 * cz + dz;
+                    if (fz < 0 || fz >= F.nz) continue;
+                    const int fi = sidx(F, fx, fy, fz);
+                    if (F.code[fi] & CODE_FLUID) sum += wxy * fw_weight(dz) * F.r[fi];
+                }
+            }
+        }
+        C.f[i] = 0.5f * sum;
+    }
+    __syncthreads();
+}
+
+// fine x += P x_coarse on fluid fine cells (coarse fluid values only)
+__device__ void s_prolong(const SLev& F, const SLev& C) {
+    for (int i = threadIdx.x; i < F.n; i += blockDim.x) {
+        if (!(F.code[i] & CODE_FLUID)) continue;
+        const int z = i % F.nz, y = (i / F.nz) % F.ny, x = i / (F.nz * F.ny);
+        const int p[3] = {(x & 1) ? x >> 1 : (x >> 1) - 1, (y & 1) ? y >> 1 : (y >> 1) - 1,
+                          (z & 1) ? z >> 1 : (z >> 1) - 1};
+        const float wl[3] = {(x & 1) ? 0.75f : 0.25f, (y & 1) ? 0.75f : 0.25f, (z & 1) ? 0.75f : 0.25f};
+        float sum = 0.f;
+        for (int o = 0; o < 8; o++) {
+            const int ox = o >> 2, oy = (o >> 1) & 1, oz = o & 1;
+            const int cx = p[0] + ox, cy = p[1] + oy, cz = p[2] + oz;
+            if (cx < 0 || cy < 0 || cz < 0 || cx >= C.nx || cy >= C.ny || cz >= C.nz) continue;
+            const int ci = sidx(C, cx, cy, cz);
+            if (!(C.code[ci] & CODE_FLUID)) continue;
+            sum += (ox ? 1.f - wl[0] : wl[0]) * (oy ? 1.f - wl[1] : wl[1]) * (oz ? 1.f - wl[2] : wl[2]) * C.x[ci];
+        }
+        F.x[i] += sum;
+    }
+    __syncthreads();
+}
+
+// V-cycle of chain levels ls..last in the block's shared memory; level ls's rhs
+// comes from global memory, its correction goes back there
+__device__ void smem_vcycle(const MGChain& C, float* smem) {
+    __shared__ SLev S[MG_MAX_LEVELS];
+    if (threadIdx.x == 0) {
+        float* p = smem;
+        for (int l = C.ls; l <= C.last; l++) {
+            const MGLev& G = C.lev[l];
+            SLev& L = S[l];
+            L.nx = G.nx; L.ny = G.ny; L.nz = G.nz;
+            L.n = G.nx * G.ny * G.nz;
+            L.x = p; p += L.n;
+            L.f = p; p += L.n;
+            L.r = p; p += L.n;
+            L.code = reinterpret_cast<uint16_t*>(p);
+            p += (L.n + 1) / 2;
+        }
+    }
+    __syncthreads();
+    for (int l = C.ls; l <= C.last; l++) {
+        const MGLev& G = C.lev[l];
+        const SLev& L = S[l];
+        for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
+            const long long gi = (long long)(i / L.nz) * G.pz + (i % L.nz);
+            L.code[i] = G.code[gi];
+            L.x[i] = 0.f;
+            if (l == C.ls) L.f[i] = G.f[gi];
+        }
+    }
+    __syncthreads();
+    for (int l = C.ls; l < C.last; l++) {
+        for (int k = 0; k < C.nu; k++) {
+            s_smooth(S[l], 0);
+            s_smooth(S[l], 1);
+        }
+        s_residual(S[l]);
+        s_restrict(S[l], S[l + 1]);
+    }
+    for (int k = 0; k < MG_BOTTOM_SWEEPS; k++) {
+        s_smooth(S[C.last], 0);
+        s_smooth(S[C.last], 1);
+    }
+    for (int k = 0; k < MG_BOTTOM_SWEEPS; k++) {
+        s_smooth(S[C.last], 1);
+        s_smooth(S[C.last], 0);
+    }
+    for (int l = C.last - 1; l >= C.ls; l--) {
+        s_prolong(S[l], S[l + 1]);
+        for (int k = 0; k < C.nu; k++) {
+            s_smooth(S[l], 1);
+            s_smooth(S[l], 0);
+        }
+    }
+    const MGLev& G = C.lev[C.ls];
+    for (int i = threadIdx.x; i < S[C.ls].n; i += blockDim.x)
+        G.x[(long long)(i / S[C.ls].nz) * G.pz + (i % S[C.ls].nz)] = S[C.ls].x[i];
+}
 
 __device__ __forceinline__ void cluster_barrier() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
@@ -1053,15 +1219,14 @@ __device__ __forceinline__ unsigned cluster_size() {
     return n;
 }
 
-constexpr int MG_POOL_FLOATS = (MG_BOTTOM_MAX * 5 + 1) / 2;  // bottom: x, f (floats) and codes
 
 __global__ void __launch_bounds__(MG_CLUSTER_THREADS) k_mg_coarse(const PcgArgs A, const __grid_constant__ MGChain C) {
     pdl_enter();
     if (A.st->done) return;  // the same value in every CTA of the cluster
-    __shared__ float pool[MG_POOL_FLOATS];
+    extern __shared__ float pool[];
     const long long i0 = (long long)cluster_rank() * blockDim.x + threadIdx.x;
     const long long step = (long long)cluster_size() * blockDim.x;
-    for (int l = C.lc; l < C.last; l++) {
+    for (int l = C.lc; l < C.ls; l++) {
         const MGLev& L = C.lev[l];
         for (int k = 0; k < C.nu; k++) {
             mg_for_range(L, i0, step, [&](int x, int y, int z0, long long c0) { smooth_quad(L, L.f, 0, k == 0, x, y, z0, c0); });
@@ -1075,10 +1240,9 @@ __global__ void __launch_bounds__(MG_CLUSTER_THREADS) k_mg_coarse(const PcgArgs 
         mg_for_range(Cl, i0, step, [&](int x, int y, int z0, long long c0) { restrict_quad(L, Cl, x, y, z0, c0); });
         cluster_barrier();
     }
-    if (cluster_rank() == 0)
-        mg_bottom_block(C.lev[C.last], pool, pool + MG_BOTTOM_MAX, reinterpret_cast<uint16_t*>(pool + 2 * MG_BOTTOM_MAX));
+    if (cluster_rank() == 0) smem_vcycle(C, pool);
     cluster_barrier();
-    for (int l = C.last - 1; l >= C.lc; l--) {
+    for (int l = C.ls - 1; l >= C.lc; l--) {
         const MGLev& L = C.lev[l];
         const MGLev& Cl = C.lev[l + 1];
         mg_for_range(L, i0, step, [&](int x, int y, int z0, long long c0) { prolong_quad(L, Cl, x, y, z0, c0); });
@@ -1231,6 +1395,7 @@ int solver_alloc(fsim_ctx* ctx) {
     }
     // cluster for the coarse V-cycle: 16 CTAs where the GPU schedules them, else 8
     S.mg_cluster = 0;
+    cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     for (int cs : {16, 8}) {
         if (cs > 8 && cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
                           cudaSuccess) {
@@ -1312,9 +1477,24 @@ static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, c
         C.lc = 0;
         C.last = last - l;
         C.nu = NUC;
+        // the levels from ls on run in shared memory (x, f, r floats + codes per cell)
+        C.ls = C.last;
+        size_t smem = 0;
+        for (int k = C.last; k >= 0; k--) {
+            const MGLevelBufs& b = S.mg[l + k];
+            const long long n = (long long)b.nx * b.ny * b.nz;
+            if (n > MG_SMEM_CELLS) break;
+            C.ls = k;
+        }
+        for (int k = C.ls; k <= C.last; k++) {
+            const MGLevelBufs& b = S.mg[l + k];
+            const long long n = (long long)b.nx * b.ny * b.nz;
+            smem += (size_t)(3 * n + (n + 1) / 2) * sizeof(float);
+        }
         cudaLaunchConfig_t cfg{};
         cfg.gridDim = dim3(S.mg_cluster);
         cfg.blockDim = dim3(MG_CLUSTER_THREADS);
+        cfg.dynamicSmemBytes = smem;
         cfg.stream = st;
         cudaLaunchAttribute at[2];
         at[0].id = cudaLaunchAttributeClusterDimension;
