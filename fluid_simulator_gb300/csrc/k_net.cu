@@ -863,7 +863,7 @@ int fsim_net_create(uint64_t seed, float out_scale, fsim_net** out) {
             !conv_wt_map(&L.mwt, L.wt, L.taps, L.cin, L.cout, conv_nt(L.taps, L.cin)))
             return bad("weight tensor maps");
     }
-    // He initialisation (fan-in of the real inputs), zero biases
+    // He initialisation (fan-in of the real inputs), zero biases, zero head
     std::vector<float> h((size_t)off, 0.f);
     uint64_t k = 0;
     for (int l = 0; l < NET_LAYERS; l++) {
@@ -875,7 +875,9 @@ int fsim_net_create(uint64_t seed, float out_scale, fsim_net** out) {
             h[(size_t)(L.w_off + i)] = (l == 0 && c >= 4) ? 0.f : (float)(sd * gauss(seed, k++));
         }
     }
-    for (int c = 0; c < 16; c++) h[(size_t)(net->head_w + c)] = (float)(std::sqrt(1.0 / 16.0) * gauss(seed, k++));
+    // the head starts at zero: the untrained network predicts the zero guess,
+    // so training (residual loss) starts from the zero start's loss and improves on it
+    for (int c = 0; c < 16; c++) h[(size_t)(net->head_w + c)] = 0.f;
     if (cudaMemcpy(net->theta, h.data(), pb, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(net->grad, 0, pb) != cudaSuccess || cudaMemset(net->adam_m, 0, pb) != cudaSuccess ||
         cudaMemset(net->adam_v, 0, pb) != cudaSuccess || cudaMemset(net->d_err, 0, 64) != cudaSuccess)

@@ -139,12 +139,23 @@ def _batch(n, size, seed):
     return np.stack(xs), np.stack(ts), np.stack(ms)
 
 
+def _random_head(net, seed=5):
+    theta = net.params()
+    _, hw, hb, _ = net_ref.layout()
+    assert not theta[hw:hb + 1].any()
+    theta[hw:hw + 16] = np.random.default_rng(seed).standard_normal(16) * 0.25
+    net.set_params(theta)
+    return net.params()
+
+
 @pytest.mark.gpu
 def test_network_forward_backward_matches_cpu(gpu):
     from fluid_simulator_gb300 import native as N
     net = N.WarmStartNet(seed=1, out_scale=2.0)
     assert net.num_params == net_ref.num_params()
-    theta = net.params()
+    # the head starts at zero (the untrained network predicts the zero guess),
+    # which would make every upstream gradient zero: give it random weights
+    theta = _random_head(net)
     x, t, m = _batch(2, 16, 10)
     out = net.forward(x, train=True)
     net.zero_grad()
@@ -181,7 +192,7 @@ def test_network_forward_backward_matches_cpu(gpu):
 def test_adam_step_matches_formula(gpu):
     from fluid_simulator_gb300 import native as N
     net = N.WarmStartNet(seed=3)
-    theta0 = net.params()
+    theta0 = _random_head(net)
     x, t, m = _batch(1, 16, 20)
     net.forward(x, train=True)
     net.zero_grad()
