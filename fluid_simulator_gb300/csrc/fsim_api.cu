@@ -160,12 +160,13 @@ DevObstacle to_dev(const fsim_ctx* ctx, const fsim_obstacle& o) {
         const GridGeom& g = ctx->g;
         const int nn[3] = {g.nx, g.ny, g.nz};
         const double pr = ctx->prm.particle_r;
+        const double hh[3] = {g.hd, g.hd, g.hzd}, hi[3] = {g.hinvd, g.hinvd, g.hzinvd};
         for (int a = 0; a < 3; a++) {
-            const double c = o.pos[a] * g.hinvd, dd = o.size[a] * g.hinvd * 0.5;
+            const double c = o.pos[a] * hi[a], dd = o.size[a] * hi[a] * 0.5;
             const int mn = (int)std::max(std::round(c - dd), 1.0);
             const int mx = (int)std::min(std::round(c + dd), nn[a] - 1.0);
-            d.box_lo[a] = (float)((double)mn * g.hd - pr);
-            d.box_hi[a] = (float)((double)mx * g.hd + pr);
+            d.box_lo[a] = (float)((double)mn * hh[a] - pr);
+            d.box_hi[a] = (float)((double)mx * hh[a] + pr);
         }
     }
     return d;
@@ -179,11 +180,14 @@ void fill_advect_args(fsim_ctx* ctx, AdvectArgs& a, double dt) {
     const GridGeom& g = ctx->g;
     const double pr = ctx->prm.particle_r;
     for (int k = 0; k < 3; k++) {
-        const double lo = g.hd + pr * 1.01;  // gridLow (simulator.cpp:140)
+        const double hk = k == 2 ? g.hzd : g.hd;
+        // gridLow (simulator.cpp:140): no radius margin on z in 2D mode
+        const double lo = hk + (k == 2 && g.two_d ? 0.0 : pr) * 1.01;
+        const double plo = hk + pr * 1.01;  // particleLow (simulator.cpp:257)
         a.lo[k] = (float)lo;
         a.hi[k] = (float)(g.dims[k] - lo);
-        a.plo[k] = a.lo[k];
-        a.phi[k] = a.hi[k];
+        a.plo[k] = (float)plo;
+        a.phi[k] = (float)(g.dims[k] - plo);
     }
     a.pr = (float)pr;
     a.despawn = ctx->prm.despawning_enabled;
@@ -229,11 +233,11 @@ int run_keys(fsim_ctx* ctx, int do_advect, int do_push, int do_stop, double dt) 
 int push_apart_pass(fsim_ctx* ctx) {
     const GridGeom& g = ctx->g;
     const double pr = ctx->prm.particle_r;
-    if (2.0 * pr > g.hd)
+    if (2.0 * pr > std::min(g.hd, g.hzd))
         return set_error(ctx, FSIM_E_UNSUPPORTED, "push-apart needs particle_r <= h/2 (neighbours within one cell)");
     float lo[3], hi[3];
     for (int k = 0; k < 3; k++) {
-        const double low = g.hd + pr * 1.01;  // particleLow (hashedParticles.cpp:67)
+        const double low = (k == 2 ? g.hzd : g.hd) + pr * 1.01;  // particleLow (hashedParticles.cpp:67)
         lo[k] = (float)low;
         hi[k] = (float)(g.dims[k] - low);
     }
@@ -291,7 +295,7 @@ int do_spawn(fsim_ctx* ctx, double dt) {
             }
         } else if (o.type == FSIM_OBS_DISC_SOURCE) {
             Job j{(int)k, 0, {}, (int)(o.pos[1] * g.hinvd)};
-            const double cx = o.pos[0] * g.hinvd, cz = o.pos[2] * g.hinvd, r = o.r * g.hinvd;
+            const double cx = o.pos[0] * g.hinvd, cz = o.pos[2] * g.hzinvd, r = o.r * g.hinvd;
             for (int x = 1; x < g.nx - 1; x++)
                 for (int z = 1; z < g.nz - 1; z++) {
                     const double dx = x + 0.5 - cx, dz = z + 0.5 - cz;
@@ -375,7 +379,6 @@ extern "C" {
 int fsim_create(const fsim_grid_desc* gd, const fsim_params* params, fsim_ctx** out) {
     if (!gd || !params || !out) return FSIM_E_INVALID;
     *out = nullptr;
-    if (gd->two_d) return FSIM_E_UNSUPPORTED;
     if (!(gd->resolution > 0) || !(gd->dims[0] > 0) || !(gd->dims[1] > 0) || !(gd->dims[2] > 0))
         return FSIM_E_INVALID;
     std::string why;
@@ -384,16 +387,23 @@ int fsim_create(const fsim_grid_desc* gd, const fsim_params* params, fsim_ctx** 
     fsim_ctx* ctx = new (std::nothrow) fsim_ctx();
     if (!ctx) return FSIM_E_OOM;
     ctx->prm = *params;
-    // MacGrid ctor (macGrid.cpp:9-13): cellD = 1 / resolution (resolution passed as float)
+    // MacGrid ctor (macGrid.cpp:9-13): cellD = 1 / resolution (resolution passed
+    // as float); in 2D mode the z axis is 3 cells of targetDimensions.z / 3 and
+    // keeps targetDimensions.z as its extent
     const double res = (double)(float)gd->resolution;
     GridGeom& g = ctx->g;
     g.hd = 1 / res;
     g.hinvd = 1.0 / g.hd;
     g.h = (float)g.hd;
     g.hinv = (float)g.hinvd;
+    g.two_d = gd->two_d ? 1 : 0;
+    g.hzd = g.two_d ? gd->dims[2] / 3 : g.hd;
+    g.hzinvd = 1.0 / g.hzd;
+    g.hz = (float)g.hzd;
+    g.hzinv = (float)g.hzinvd;
     g.nx = (int)(gd->dims[0] / g.hd);
     g.ny = (int)(gd->dims[1] / g.hd);
-    g.nz = (int)(gd->dims[2] / g.hd);
+    g.nz = g.two_d ? 3 : (int)(gd->dims[2] / g.hd);
     if (g.nx < 3 || g.ny < 3 || g.nz < 3) {
         delete ctx;
         return FSIM_E_INVALID;
@@ -402,7 +412,8 @@ int fsim_create(const fsim_grid_desc* gd, const fsim_params* params, fsim_ctx** 
     g.ncell = (long long)g.nx * g.ny * g.pz;
     g.dims[0] = g.nx * g.hd;
     g.dims[1] = g.ny * g.hd;
-    g.dims[2] = g.nz * g.hd;
+    g.dims[2] = g.two_d ? gd->dims[2] : g.nz * g.hd;
+    g.zc = (float)(gd->dims[2] / 2);
     if (!(ctx->prm.particle_r > 0)) ctx->prm.particle_r = g.hd / 4.0;
 
     auto fail = [&](int code, const char* msg) {
@@ -487,7 +498,7 @@ int fsim_get_params(fsim_ctx* ctx, fsim_params* out) {
 int fsim_grid_info(fsim_ctx* ctx, int* n3, double* h3, double* dims3) {
     if (!ctx) return FSIM_E_INVALID;
     if (n3) { n3[0] = ctx->g.nx; n3[1] = ctx->g.ny; n3[2] = ctx->g.nz; }
-    if (h3) { h3[0] = h3[1] = h3[2] = ctx->g.hd; }
+    if (h3) { h3[0] = h3[1] = ctx->g.hd; h3[2] = ctx->g.hzd; }
     if (dims3) for (int a = 0; a < 3; a++) dims3[a] = ctx->g.dims[a];
     return FSIM_OK;
 }

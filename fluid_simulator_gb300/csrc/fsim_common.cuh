@@ -27,9 +27,13 @@
 struct GridGeom {
     int nx, ny, nz, pz;
     long long ncell;   // nx * ny * pz
-    float h, hinv;
+    float h, hinv;     // cellD.x = cellD.y
     double hd, hinvd;
+    float hz, hzinv;   // cellD.z: h, or targetDimensions.z / 3 in 2D mode (macGrid.cpp:10)
+    double hzd, hzinvd;
     double dims[3];    // MacGrid::dimensions
+    int two_d;         // 2D mode: 3 cells in z, particles held at z = zc, no z motion
+    float zc;          // HashedParticles::z = targetDimensions.z / 2 (simulationManager.cpp:27)
 };
 
 __host__ __device__ inline long long gidx(const GridGeom& g, int x, int y, int z) {

@@ -75,6 +75,10 @@ extern "C" int fsim_p2g_noalloc(const fsim_grid_desc* grid, int transfer, const 
     g.hinvd = 1.0 / g.hd;
     g.h = (float)g.hd;
     g.hinv = (float)g.hinvd;
+    g.hzd = g.hd;
+    g.hzinvd = g.hinvd;
+    g.hz = g.h;
+    g.hzinv = g.hinv;
     g.nx = (int)(grid->dims[0] / g.hd);
     g.ny = (int)(grid->dims[1] / g.hd);
     g.nz = (int)(grid->dims[2] / g.hd);

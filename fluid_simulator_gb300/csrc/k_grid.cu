@@ -274,14 +274,14 @@ __global__ void k_copy_phi(GridGeom g, const double* phi, float* out) {
 int launch_obstacle(fsim_ctx* ctx, const fsim_obstacle& ob) {
     const GridGeom& g = ctx->g;
     ObsGeom o;
-    const double hinv = g.hinvd;
-    const double cx = ob.pos[0] * hinv, cy = ob.pos[1] * hinv, cz = ob.pos[2] * hinv;
+    const double hinv = g.hinvd, hinv_a[3] = {g.hinvd, g.hinvd, g.hzinvd};
+    const double cx = ob.pos[0] * hinv, cy = ob.pos[1] * hinv, cz = ob.pos[2] * g.hzinvd;
     for (int a = 0; a < 3; a++) o.speed[a] = (float)ob.speed[a];
     const int nn[3] = {g.nx, g.ny, g.nz};
     const double cc[3] = {cx, cy, cz};
     if (ob.type == FSIM_OBS_SPHERE || ob.type == FSIM_OBS_SOURCE) {
         o.kind = 0;
-        const double r = hinv * ob.r;
+        const double r = hinv * ob.r;  // cellDInv.x * r, on every axis
         o.cx = cx; o.cy = cy; o.cz = cz;
         o.r2 = r * r;
         for (int a = 0; a < 3; a++) {
@@ -292,7 +292,7 @@ int launch_obstacle(fsim_ctx* ctx, const fsim_obstacle& ob) {
         o.kind = 1;
         o.cx = o.cy = o.cz = o.r2 = 0;
         for (int a = 0; a < 3; a++) {
-            const double d = ob.size[a] * hinv * 0.5;
+            const double d = ob.size[a] * hinv_a[a] * 0.5;
             o.mn[a] = (int)std::max(std::round(cc[a] - d), 1.0);
             o.mx[a] = (int)std::min(std::round(cc[a] + d), nn[a] - 1.0);
         }

@@ -168,15 +168,19 @@ __global__ void __launch_bounds__(256) k_advect(const AdvectArgs a) {
                         const float dist = sqrtf(d2);
                         px = clampf(o.pos[0] + dx / dist * r, a.plo[0], a.phi[0]);
                         py = clampf(o.pos[1] + dy / dist * r, a.plo[1], a.phi[1]);
-                        pz = clampf(o.pos[2] + dz / dist * r, a.plo[2], a.phi[2]);
+                        // zConst (simulator.cpp:276): 2D particles go back to the plane
+                        pz = a.g.two_d ? a.g.zc : clampf(o.pos[2] + dz / dist * r, a.plo[2], a.phi[2]);
                     }
                 } else if (o.type == FSIM_OBS_BOX) {
+                    // in 2D the z extent is not tested and z is never the push axis
+                    // (simulator.cpp:285-290)
                     if (!(px > o.box_hi[0] || px < o.box_lo[0] || py > o.box_hi[1] || py < o.box_lo[1] ||
-                          pz > o.box_hi[2] || pz < o.box_lo[2])) {
+                          ((pz > o.box_hi[2] || pz < o.box_lo[2]) && !a.g.two_d))) {
                         float pp[3] = {px, py, pz};
                         int axis = 0;
                         float amount = 1e6f;
-                        for (int q = 0; q < 3; q++) {
+                        const int naxes = a.g.two_d ? 2 : 3;
+                        for (int q = 0; q < naxes; q++) {
                             if (pp[q] > o.pos[q]) {
                                 float tmp = o.box_hi[q] - pp[q];
                                 if (tmp < fabsf(amount)) { amount = tmp; axis = q; }
@@ -201,7 +205,7 @@ __global__ void __launch_bounds__(256) k_advect(const AdvectArgs a) {
             a.p.v[0][i] = vx; a.p.v[1][i] = vy; a.p.v[2][i] = vz;
         }
         if (a.do_key && !dead) {
-            int cx = (int)(px * a.g.hinv), cy = (int)(py * a.g.hinv), cz = (int)(pz * a.g.hinv);
+            int cx = (int)(px * a.g.hinv), cy = (int)(py * a.g.hinv), cz = (int)(pz * a.g.hzinv);
             cx = min(max(cx, 0), a.g.nx - 1);
             cy = min(max(cy, 0), a.g.ny - 1);
             cz = min(max(cz, 0), a.g.nz - 1);
@@ -324,7 +328,7 @@ __global__ void k_push_apart(ParticleBuf p, const uint32_t* perm, const int* cst
     if (k >= live || k >= n) return;
     const uint32_t i = perm[k];
     const float xi = p.p[0][i], yi = p.p[1][i], zi = p.p[2][i];
-    const int cx = (int)(xi * g.hinv), cy = (int)(yi * g.hinv), cz = (int)(zi * g.hinv);
+    const int cx = (int)(xi * g.hinv), cy = (int)(yi * g.hinv), cz = (int)(zi * g.hzinv);
     const float D = 2.f * r, D2 = D * D;
     float dx = 0.f, dy = 0.f, dz = 0.f;
     for (int ox = -1; ox <= 1; ox++) {
@@ -353,7 +357,7 @@ __global__ void k_push_apart(ParticleBuf p, const uint32_t* perm, const int* cst
     }
     out0[i] = fminf(fmaxf(xi + dx, lo0), hi0);
     out1[i] = fminf(fmaxf(yi + dy, lo1), hi1);
-    out2[i] = fminf(fmaxf(zi + dz, lo2), hi2);
+    out2[i] = g.two_d ? g.zc : fminf(fmaxf(zi + dz, lo2), hi2);  // zConst (hashedParticles.cpp:98)
 }
 
 __global__ void k_scatter(const uint32_t* key, const uint32_t* rank, const int* cstart, uint32_t* perm,
@@ -409,9 +413,10 @@ __global__ void k_spawn_sphere(ParticleBuf p, long long first, int count, double
 }
 
 // Disc source (extension): 8 particles per covered cell, one per 2x2x2
-// sub-cell with +-0.5 sub-cell jitter, velocity (0, speed, 0).
+// sub-cell with +-0.5 sub-cell jitter, velocity (0, speed, 0).  In 2D mode the
+// particles sit on the plane z = zc.
 __global__ void k_spawn_disc(ParticleBuf p, long long first, int ncells, const int* cells_xz, int cy,
-                             float h, float vy, uint64_t seed, uint32_t first_id, int ids) {
+                             GridGeom g, float vy, uint64_t seed, uint32_t first_id, int ids) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= ncells * 8) return;
     const int c = k >> 3, s = k & 7;
@@ -422,8 +427,9 @@ __global__ void k_spawn_disc(ParticleBuf p, long long first, int ncells, const i
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         double u = uniform01(seed, 3ull * k + a);
-        p.p[a][i] = (float)((base[a] + sub[a] + (u - 0.5) * 0.5 * 0.999) * h);
+        p.p[a][i] = (float)((base[a] + sub[a] + (u - 0.5) * 0.5 * 0.999) * (a == 2 ? g.hzd : g.hd));
     }
+    if (g.two_d) p.p[2][i] = g.zc;
     p.v[0][i] = 0.f;
     p.v[1][i] = vy;
     p.v[2][i] = 0.f;
@@ -439,7 +445,7 @@ __global__ void k_gfx(ParticleBuf p, long long n, const float* avg, GridGeom g, 
     if (i >= n) return;
     const float px = p.p[0][i], py = p.p[1][i], pz = p.p[2][i];
     const float vx = p.v[0][i], vy = p.v[1][i], vz = p.v[2][i];
-    const float gx = px * g.hinv - 0.5f, gy = py * g.hinv - 0.5f, gz = pz * g.hinv - 0.5f;
+    const float gx = px * g.hinv - 0.5f, gy = py * g.hinv - 0.5f, gz = pz * g.hzinv - 0.5f;
     const int bx = (int)gx, by = (int)gy, bz = (int)gz;
     float dens = 0.f;
 #pragma unroll
@@ -502,7 +508,7 @@ void launch_spawn_disc(ParticleBuf p, long long first, int ncells, const fsim_ob
                        const GridGeom& g, int cy, const int* cells_xz, uint64_t seed,
                        uint32_t first_id, bool ids, cudaStream_t s) {
     if (ncells <= 0) return;
-    k_spawn_disc<<<ceil_div(ncells * 8, 128), 128, 0, s>>>(p, first, ncells, cells_xz, cy, g.h,
+    k_spawn_disc<<<ceil_div(ncells * 8, 128), 128, 0, s>>>(p, first, ncells, cells_xz, cy, g,
                                                            (float)o.spawn_speed, seed, first_id,
                                                            ids ? 1 : 0);
 }

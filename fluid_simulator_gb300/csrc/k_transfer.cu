@@ -26,7 +26,6 @@
 namespace {
 
 constexpr int TX = 8, TY = 8, TZ = 32;
-constexpr int P2G_THREADS = 256;
 
 // G2P staged box: x in [x0-1, x0+TX], y in [y0-1, y0+TY], z in [z0-4, z0+TZ+4)
 constexpr int BX = TX + 2, BY = TY + 2, BZ = TZ + 8;
@@ -78,16 +77,17 @@ constexpr int NACC = 72;
 
 template <bool APIC, int AX, int OW, int OV>
 __device__ __forceinline__ void p2g_face_axis(const float (&f)[3], const float (&wt)[3][3], float va,
-                                              const float* cm, float h, float (&acc)[NACC]) {
+                                              const float* cm, float h, float zr, float (&acc)[NACC]) {
     constexpr int b = AX == 0 ? 1 : 0, c = AX == 2 ? 1 : 2;  // transverse axes, increasing
     const float wn[2] = {1.f - f[AX], f[AX]};
     float K = va, ka = 0.f, kb = 0.f, kc = 0.f;
     if (APIC) {
-        // contribution v_a + c[a] . (face - pos) = K + h (c_a ii + c_b (j - 1/2) + c_c (k - 1/2))
-        K -= h * (cm[0] * f[0] + cm[1] * f[1] + cm[2] * f[2]);
-        ka = h * cm[AX];
+        // contribution v_a + c[a] . (face - pos) = K + h (c_a ii + c_b (j - 1/2) + c_c (k - 1/2)),
+        // with the z terms scaled by zr = cellD.z / cellD.x (1 except in 2D mode)
+        K -= h * (cm[0] * f[0] + cm[1] * f[1] + cm[2] * f[2] * zr);
+        ka = h * cm[AX] * (AX == 2 ? zr : 1.f);
         kb = h * cm[b];
-        kc = h * cm[c];
+        kc = h * cm[c] * (c == 2 ? zr : 1.f);
     }
 #pragma unroll
     for (int j = 0; j < 3; j++)
@@ -135,7 +135,8 @@ __global__ void __launch_bounds__(P2G_THREADS_V2, 1) k_p2g(const P2GArgs a) {
     const int tz = bt % a.ntz, ty = (bt / a.ntz) % a.nty, tx = bt / (a.ntz * a.nty);
     const int x0 = tx * PX, y0 = ty * PY, z0 = tz * PZ;
     __syncthreads();
-    const float hinv = a.g.hinv, h = a.g.h;
+    const float hinv = a.g.hinv, h = a.g.h, zr = a.g.two_d ? (float)(a.g.hzd * a.g.hinvd) : 1.f;
+    const float hinv3[3] = {hinv, hinv, a.g.hzinv};
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int role = warp & 1;                  // 0: x faces + density, 1: y and z faces
     const int pairs = P2G_THREADS_V2 / 64;      // warp pairs per CTA
@@ -159,7 +160,7 @@ __global__ void __launch_bounds__(P2G_THREADS_V2, 1) k_p2g(const P2GArgs a) {
             const uint32_t i = a.perm[k];
             float f[3];
 #pragma unroll
-            for (int d = 0; d < 3; d++) f[d] = a.p.p[d][i] * hinv - (float)cc[d];
+            for (int d = 0; d < 3; d++) f[d] = a.p.p[d][i] * hinv3[d] - (float)cc[d];
             float wt[3][3];
 #pragma unroll
             for (int d = 0; d < 3; d++) tent3(f[d], wt[d]);
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(P2G_THREADS_V2, 1) k_p2g(const P2GArgs a) {
 #pragma unroll
                     for (int q = 0; q < 3; q++) cm[q] = a.p.c[q][i];
                 }
-                p2g_face_axis<APIC, 0, 0, 18>(f, wt, a.p.v[0][i], cm, h, acc);
+                p2g_face_axis<APIC, 0, 0, 18>(f, wt, a.p.v[0][i], cm, h, zr, acc);
 #pragma unroll
                 for (int ox = 0; ox < 3; ox++)
 #pragma unroll
@@ -187,8 +188,8 @@ __global__ void __launch_bounds__(P2G_THREADS_V2, 1) k_p2g(const P2GArgs a) {
                         cmz[q] = a.p.c[6 + q][i];
                     }
                 }
-                p2g_face_axis<APIC, 1, 0, 18>(f, wt, a.p.v[1][i], cmy, h, acc);
-                p2g_face_axis<APIC, 2, 36, 54>(f, wt, a.p.v[2][i], cmz, h, acc);
+                p2g_face_axis<APIC, 1, 0, 18>(f, wt, a.p.v[1][i], cmy, h, zr, acc);
+                p2g_face_axis<APIC, 2, 36, 54>(f, wt, a.p.v[2][i], cmz, h, zr, acc);
             }
         }
         if (role == 0) {
@@ -337,7 +338,7 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
         }
     }
     const int total = seg_pre[TX * TY];
-    const float hinv = a.g.hinv;
+    const float hinv = a.g.hinv, hzinv = a.g.hzinv;
     for (int j = threadIdx.x; j < total; j += blockDim.x) {
         int lo = 0, hi = TX * TY - 1;
         while (lo < hi) {
@@ -347,7 +348,7 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
         const int k = seg_beg[lo] + (j - seg_pre[lo]);
         const uint32_t i = a.perm[k];
         const float px = a.src.p[0][i], py = a.src.p[1][i], pz = a.src.p[2][i];
-        const float g[3] = {px * hinv, py * hinv, pz * hinv};
+        const float g[3] = {px * hinv, py * hinv, pz * hzinv};
         float vnew[3];
         float cnew[9];
 #pragma unroll
@@ -375,9 +376,18 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
                 if (MODE == 1) flip += (v2 - su[ax * BOXN + si]) * w;
                 if (MODE == 2) {
                     // trilinearInterpollGradient (util/interpolation.h:21-35)
+                    float sz_ = dz > 0.f ? -1.f : 1.f;
+                    if (a.g.two_d) {
+                        // 2D particles sit on the z node plane, where the sign flips: take it
+                        // from the FP64 offset as the reference does (0.15f * 10 rounds to
+                        // exactly 1.5 in FP32, 6e-8 above it in FP64)
+                        const double e = ((double)pz - ((double)(b[2] + oz) + (ax == 2 ? 1.0 : 0.5)) * a.g.hzd) *
+                                         a.g.hzinvd;
+                        sz_ = e > 0.0 ? -1.f : 1.f;
+                    }
                     const float gx = (dx > 0.f ? -1.f : 1.f) * wy * wz * hinv;
                     const float gy = (dy > 0.f ? -1.f : 1.f) * wx * wz * hinv;
-                    const float gz = (dz > 0.f ? -1.f : 1.f) * wx * wy * hinv;
+                    const float gz = sz_ * wx * wy * hzinv;
                     c0 += gx * v2;
                     c1 += gy * v2;
                     c2 += gz * v2;
@@ -390,6 +400,14 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
                 cnew[3 * ax] = c0;
                 cnew[3 * ax + 1] = c1;
                 cnew[3 * ax + 2] = c2;
+            }
+        }
+        if (a.g.two_d) {
+            // 2D mode (simulator.cpp:382-385): v.z = 0 and the z row of C is left as it was
+            vnew[2] = 0.f;
+            if (MODE == 2) {
+#pragma unroll
+                for (int q = 6; q < 9; q++) cnew[q] = a.src.c[q][i];
             }
         }
         a.dst.p[0][k] = px;

@@ -206,12 +206,13 @@ def _ptr(a):
 class Simulation:
     """One simulation context on the current CUDA device."""
 
-    def __init__(self, resolution: float, params: Params, *, dims=(1.0, 1.0, 1.0), track_ids: bool = False):
+    def __init__(self, resolution: float, params: Params, *, dims=(1.0, 1.0, 1.0), track_ids: bool = False,
+                 two_d: bool = False):
         self.lib = load_library()
         g = GridDesc()
         g.dims[:] = list(dims)
         g.resolution = resolution
-        g.two_d = 0
+        g.two_d = int(two_d)
         params.track_ids = int(track_ids)
         self.params = params
         self.ctx = C.c_void_p()
@@ -224,6 +225,8 @@ class Simulation:
         self.lib.fsim_grid_info(self.ctx, n3, h3, d3)
         self.shape = (n3[0], n3[1], n3[2])
         self.h = h3[0]
+        self.hz = h3[2]
+        self.two_d = bool(two_d)
         self.dims = (d3[0], d3[1], d3[2])
 
     def _check(self, rc: int, what: str):

@@ -50,15 +50,20 @@ class GridSpec:
 
     resolution: float
     dims: tuple = (1.0, 1.0, 1.0)
+    two_d: bool = False  # 2D mode: z is 3 cells of dims[2] / 3
 
     @property
     def h(self) -> float:
         return 1.0 / float(np.float32(self.resolution))
 
     @property
+    def hz(self) -> float:
+        return self.dims[2] / 3 if self.two_d else self.h
+
+    @property
     def shape(self) -> tuple:
         h = self.h
-        return tuple(int(d / h) for d in self.dims)
+        return (int(self.dims[0] / h), int(self.dims[1] / h), 3 if self.two_d else int(self.dims[2] / h))
 
 
 def dam_break(grid: GridSpec, block_lo=(0.0, 0.0, 0.0), block_hi=(0.4, 0.6, 1.0), seed: int = 0,
@@ -79,6 +84,29 @@ def dam_break(grid: GridSpec, block_lo=(0.0, 0.0, 0.0), block_hi=(0.4, 0.6, 1.0)
         u = uniform01(seed, 0, pos.size).reshape(-1, 3)
         pos = pos + (u - 0.5) * 0.5 * 0.999
     return (pos * h).astype(np.float32)
+
+
+def dam_break_2d(grid: GridSpec, block_lo=(0.0, 0.0), block_hi=(0.4, 0.6), seed: int = 0) -> np.ndarray:
+    """FP32 positions (n, 3) for a 2D-mode dam break: interior cells of the x-y
+    plane whose centre lies in the block, 4 particles per cell (2x2 sub-cells,
+    +-0.5 sub-cell jitter), all at z = dims[2] / 2 (HashedParticles' zConst
+    plane, simulationManager.cpp:27)."""
+    assert grid.two_d
+    h = grid.h
+    nx, ny, _ = grid.shape
+    axes = []
+    for a, n in enumerate((nx, ny)):
+        idx = np.arange(1, n - 1)
+        centre = (idx + 0.5) * h
+        axes.append(idx[(centre >= block_lo[a]) & (centre <= block_hi[a])])
+    ix, iy = np.meshgrid(*axes, indexing="ij")
+    cells = np.stack([ix.ravel(), iy.ravel()], axis=1).astype(np.float64)
+    sub = np.array([[sx, sy] for sx in (0.25, 0.75) for sy in (0.25, 0.75)])
+    xy = (cells[:, None, :] + sub[None, :, :]).reshape(-1, 2)
+    u = uniform01(seed, 0, xy.size).reshape(-1, 2)
+    xy = (xy + (u - 0.5) * 0.5 * 0.999) * h
+    z = np.full((xy.shape[0], 1), grid.dims[2] / 2)
+    return np.concatenate([xy, z], axis=1).astype(np.float32)
 
 
 def fill_below(grid: GridSpec, y_top: float, seed: int = 0) -> np.ndarray:

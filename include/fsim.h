@@ -134,7 +134,8 @@ enum fsim_field {
 typedef struct fsim_grid_desc {
     double dims[3];    /* target dimensions */
     double resolution; /* cells per unit length (rounded to float as BridsonSolverGrid does) */
-    int two_d;         /* must be 0: 2D mode is not built */
+    int two_d;         /* 2D mode: z is 3 cells of dims[2] / 3, particles stay on z = dims[2] / 2,
+                          G2P sets v.z = 0 (macGrid.cpp:9-13, simulator.cpp:382-385) */
 } fsim_grid_desc;
 
 /* Simulator::SimulatorConfig (simulator.h:30-39) + MacGrid public fields

@@ -555,6 +555,7 @@ static void stage_push_apart(sim *s) {
         q.x = q.x < lo[0] ? lo[0] : (q.x > hi[0] ? hi[0] : q.x);
         q.y = q.y < lo[1] ? lo[1] : (q.y > hi[1] ? hi[1] : q.y);
         q.z = q.z < lo[2] ? lo[2] : (q.z > hi[2] ? hi[2] : q.z);
+        if (s->p.two_d) q.z = s->p.dims[2] / 2; /* zConst (hashedParticles.cpp:98) */
         np[i] = q;
     }
     for (int i = 0; i < n; i++) s->pt[i].pos = np[i];

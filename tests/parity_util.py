@@ -25,18 +25,20 @@ TRANSFER_O = {N.PIC: O.PIC, N.FLIP: O.FLIP, N.APIC: O.APIC}
 
 
 def make_pair(pos, resolution, transfer, *, vel=None, c=None, lib="port", threads=0, tol=1e-6,
-              max_iters=200, gpu_tol=None, gpu_tol_mode=N.TOL_ABS_MAX, gpu_max_iters=None, **kw):
+              max_iters=200, gpu_tol=None, gpu_tol_mode=N.TOL_ABS_MAX, gpu_max_iters=None, dims=(1.0, 1.0, 1.0),
+              two_d=False, **kw):
     """(gpu Simulation, oracle) on identical FP32 particles."""
     pos = np.ascontiguousarray(pos, np.float32)
     p = N.default_params(transfer=transfer, resolution=resolution, tol=tol if gpu_tol is None else gpu_tol,
                          tol_mode=gpu_tol_mode, max_iters=max_iters if gpu_max_iters is None else gpu_max_iters,
                          **kw)
-    g = N.Simulation(resolution, p, track_ids=True)
+    g = N.Simulation(resolution, p, track_ids=True, dims=dims, two_d=two_d)
     g.set_particles(pos, vel, None if c is None else np.asarray(c, np.float32).reshape(-1, 9))
     okw = {k: v for k, v in kw.items() if k in ("spawning", "despawning", "stop_particles", "gravity",
                                                 "flip_ratio", "top_solid", "pressure_enabled", "grid_solver",
                                                 "push_apart")}
-    op = O.make_params(resolution, transfer=TRANSFER_O[transfer], tol=tol, max_iters=max_iters, **okw)
+    op = O.make_params(resolution, transfer=TRANSFER_O[transfer], tol=tol, max_iters=max_iters, dims=dims,
+                       two_d=two_d, **okw)
     o = O.Oracle(op, pos.astype(np.float64),
                  None if vel is None else np.asarray(vel, np.float32).astype(np.float64),
                  None if c is None else np.asarray(c, np.float32).astype(np.float64), lib=lib)
