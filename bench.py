@@ -412,7 +412,10 @@ def warm_start_study(sim, dt, t, h, N, args):
     (the reference), the previous step's pressure, and the judged learned guess."""
     net, info = train_warm_start(N, args)
     sim.set_net(net)
-    modes = (("zero", N.WARM_ZERO), ("previous", N.WARM_PREVIOUS), ("learned", N.WARM_LEARNED))
+    # "learned" judges the network on every solve; "learned_backoff" skips it for
+    # 1, 2, 4 ... solves after each rejection (fsim_params.learned_backoff)
+    modes = (("zero", N.WARM_ZERO), ("previous", N.WARM_PREVIOUS), ("learned", N.WARM_LEARNED),
+             ("learned_backoff", N.WARM_LEARNED))
     rec = {k: [] for k, _ in modes}
     stages = (N.STAGE_SPAWN, N.STAGE_ADVECT, N.STAGE_PUSH_OUT, N.STAGE_P2G, N.STAGE_OBSTACLES, N.STAGE_WALLS,
               N.STAGE_POST_P2G)
@@ -423,7 +426,13 @@ def warm_start_study(sim, dt, t, h, N, args):
         p_prev = sim.grid(N.F_PRESSURE)
         for name, mode in modes:
             sim.set_grid(N.F_PRESSURE, p_prev)
+            if name == "learned_backoff":
+                sim.params.learned_backoff = 1
+                sim.set_params(sim.params)
             st = sim.solve_current(dt, mode, apply=False)
+            if name == "learned_backoff":
+                sim.params.learned_backoff = 0
+                sim.set_params(sim.params)
             if k > 0:  # the first problem also pays the network's workspace allocation
                 rec[name].append((st.ms_solve, st.pcg_iterations, st.guess_used, st.ms_guess, st.residual_rel))
         sim.set_grid(N.F_PRESSURE, p_prev)
@@ -439,10 +448,12 @@ def warm_start_study(sim, dt, t, h, N, args):
         out[name] = {"ms": round(statistics.mean(x[0] for x in r), 3),
                      "iterations": round(statistics.mean(x[1] for x in r), 2),
                      "residual_rel": max(x[4] for x in r)}
-    lr = rec["learned"]
-    out["learned"]["guess_used_frac"] = round(sum(1 for x in lr if x[2] == N.WARM_LEARNED) / len(lr), 3)
-    out["learned"]["ms_guess"] = round(statistics.mean(x[3] for x in lr), 3)
-    out["speedup_vs_zero"] = {k: round(out["zero"]["ms"] / out[k]["ms"], 3) for k in ("previous", "learned")}
+    for k in ("learned", "learned_backoff"):
+        lr = rec[k]
+        out[k]["guess_used_frac"] = round(sum(1 for x in lr if x[2] == N.WARM_LEARNED) / len(lr), 3)
+        out[k]["ms_guess"] = round(statistics.mean(x[3] for x in lr), 3)
+    out["speedup_vs_zero"] = {k: round(out["zero"]["ms"] / out[k]["ms"], 3)
+                              for k in ("previous", "learned", "learned_backoff")}
     return out
 
 

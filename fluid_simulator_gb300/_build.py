@@ -20,6 +20,8 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "-diag-suppress", "177", f"-I{os.path.join(ROOT, 'include')}"]
+# the renderer rounds like its C restatement (no multiply-add contraction)
+FILE_FLAGS = {"k_render.cu": ["--fmad=false"]}
 
 
 def _sources():
@@ -28,7 +30,7 @@ def _sources():
 
 def _deps():
     return sorted(glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) +
-                  [os.path.join(ROOT, "include", "fsim.h")])
+                  glob.glob(os.path.join(ROOT, "include", "*.h")))
 
 
 def _compile(src: str) -> str:
@@ -36,7 +38,7 @@ def _compile(src: str) -> str:
     dep_mtime = max(os.path.getmtime(p) for p in _deps() + [src])
     if os.path.exists(obj) and os.path.getmtime(obj) >= dep_mtime:
         return obj
-    cmd = [NVCC, *ARCH, *FLAGS, "-c", src, "-o", obj]
+    cmd = [NVCC, *ARCH, *FLAGS, *FILE_FLAGS.get(os.path.basename(src), []), "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")

@@ -118,6 +118,8 @@ struct fsim_ctx {
     int* h_misc = nullptr;   // pinned
 
     fsim_net* net = nullptr;  // warm-start network (FSIM_WARM_LEARNED), not owned
+    int learned_skip = 0;     // solves left before the network is judged again (learned_backoff)
+    int learned_wait = 0;     // the current back-off length
 
     cudaEvent_t ev[16];
     bool events = false;

@@ -1751,12 +1751,18 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     sa.flags = ctx->flags;
     for (int a = 0; a < 3; a++) sa.v2[a] = ctx->v2[a];
     sa.avg = ctx->avg;
-    // a user or learned guess is judged against the previous pressure after setup
-    const bool judged = warm == FSIM_WARM_LEARNED || (warm == FSIM_WARM_GUESS && S.have_guess);
     if (warm == FSIM_WARM_LEARNED && !ctx->net) {
         ctx->err = "FSIM_WARM_LEARNED needs a network (fsim_set_net)";
         return FSIM_E_STATE;
     }
+    // back-off: a network whose guesses keep losing to the previous pressure is
+    // skipped (not run) for a growing number of solves
+    if (warm == FSIM_WARM_LEARNED && ctx->prm.learned_backoff && ctx->learned_skip > 0) {
+        ctx->learned_skip--;
+        warm = FSIM_WARM_PREVIOUS;
+    }
+    // a user or learned guess is judged against the previous pressure after setup
+    const bool judged = warm == FSIM_WARM_LEARNED || (warm == FSIM_WARM_GUESS && S.have_guess);
     sa.guess = nullptr;
     sa.rhs_override = rhs_override;
     sa.warm = (warm == FSIM_WARM_ZERO) ? FSIM_WARM_ZERO : FSIM_WARM_PREVIOUS;
@@ -1833,6 +1839,14 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     }
     if (rc) return rc;
     PcgState& hs = *S.st_host;
+    if (warm == FSIM_WARM_LEARNED && ctx->prm.learned_backoff) {
+        if (hs.guess_used) {
+            ctx->learned_wait = 0;
+        } else {
+            ctx->learned_wait = ctx->learned_wait ? std::min(2 * ctx->learned_wait, 64) : 1;
+            ctx->learned_skip = ctx->learned_wait;
+        }
+    }
     if (stats) {
         stats->residual_max = hs.rmax * scale;
         stats->residual_rel = hs.bb > 0 ? sqrt(hs.rr / hs.bb) : 0.0;

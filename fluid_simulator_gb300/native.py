@@ -48,7 +48,7 @@ class Params(C.Structure):
         ("tol_mode", C.c_int), ("particle_r", C.c_double), ("precision", C.c_int),
         ("warm_start", C.c_int), ("track_ids", C.c_int), ("timing", C.c_int), ("precond", C.c_int),
         ("mg_sweeps", C.c_int), ("mg_coarse_sweeps", C.c_int), ("mg_cluster_sweeps", C.c_int),
-        ("grid_solver", C.c_int), ("reserved", C.c_int * 2),
+        ("grid_solver", C.c_int), ("learned_backoff", C.c_int), ("reserved", C.c_int * 1),
     ]
 
 
@@ -78,7 +78,33 @@ class StepStats(C.Structure):
     ]
 
 
-# exported symbols, in the order include/fsim.h declares them
+# ---- renderer structures (include/fsim_render.h) ----
+RENDER_MAX_LIGHTS = 8
+IMG_COLOR, IMG_DEPTH, IMG_THICKNESS, IMG_NORMAL_DEPTH, IMG_RAW_DEPTH = 0, 1, 2, 3, 4
+
+
+class Camera(C.Structure):
+    _fields_ = [("view", C.c_float * 16), ("view_inv", C.c_float * 16), ("proj", C.c_float * 16),
+                ("proj_inv", C.c_float * 16), ("position", C.c_float * 4)]
+
+
+class Light(C.Structure):
+    _fields_ = [("position", C.c_float * 4), ("power_density", C.c_float * 3)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [
+        ("particle_radius", C.c_float), ("particle_color", C.c_float * 3), ("specular_color", C.c_float * 3),
+        ("shininess", C.c_float), ("bilateral_filter", C.c_int), ("smoothing_size", C.c_float),
+        ("blur_scale", C.c_float), ("blur_depth_falloff", C.c_float), ("spray_enabled", C.c_int),
+        ("spray_density_threshold", C.c_float), ("transparency_enabled", C.c_int),
+        ("transparency_blur_size", C.c_float), ("transparency", C.c_float), ("noise_enabled", C.c_int),
+        ("noise_scale", C.c_float), ("noise_strength", C.c_float), ("noise_offset", C.c_float),
+        ("num_lights", C.c_int), ("lights", Light * RENDER_MAX_LIGHTS), ("background", C.c_float * 4),
+    ]
+
+
+# exported symbols, in the order include/fsim.h and include/fsim_render.h declare them
 EXPORTS = [
     "fsim_create", "fsim_destroy", "fsim_set_params", "fsim_get_params", "fsim_grid_info",
     "fsim_last_error", "fsim_stream", "fsim_synchronize", "fsim_set_particles", "fsim_add_particles",
@@ -89,6 +115,8 @@ EXPORTS = [
     "fsim_net_get_params", "fsim_net_set_params", "fsim_net_forward", "fsim_net_backward",
     "fsim_net_set_loss", "fsim_net_zero_grad", "fsim_net_adam", "fsim_net_train_step", "fsim_net_synchronize",
     "fsim_net_conv", "fsim_set_net",
+    "fsim_render_default_params", "fsim_render_camera", "fsim_render_create", "fsim_render_destroy",
+    "fsim_render_last_error", "fsim_render_frame", "fsim_render_ctx", "fsim_render_read", "fsim_render_stats",
 ]
 
 _lib = None
@@ -145,6 +173,16 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "fsim_net_conv": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                     P, P, P, P, C.c_int]),
         "fsim_set_net": (C.c_int, [P, P]),
+        "fsim_render_default_params": (None, [C.POINTER(RenderParams)]),
+        "fsim_render_camera": (None, [C.POINTER(Camera), dp, C.c_double, C.c_double, C.c_double, C.c_double,
+                                      C.c_double, C.c_double]),
+        "fsim_render_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(P)]),
+        "fsim_render_destroy": (C.c_int, [P]),
+        "fsim_render_last_error": (C.c_char_p, [P]),
+        "fsim_render_frame": (C.c_int, [P, P, i64, C.c_int, C.POINTER(Camera), C.POINTER(RenderParams), P, P]),
+        "fsim_render_ctx": (C.c_int, [P, P, C.POINTER(Camera), C.POINTER(RenderParams), P]),
+        "fsim_render_read": (C.c_int, [P, C.c_int, P, C.c_int]),
+        "fsim_render_stats": (C.c_int, [P, fp, C.POINTER(C.c_int)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -166,7 +204,7 @@ def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: 
                    pressure_enabled: bool = False, pressure_k: float = 2.0, average_pressure: float = 2.0,
                    fluid_density: float = 1.0, timing: bool = False, precond: int = PRECOND_MG,
                    mg_sweeps: int = 0, mg_coarse_sweeps: int = 0, mg_cluster_sweeps: int = 0,
-                   grid_solver: int = SOLVER_PCG, push_apart: bool = False) -> Params:
+                   grid_solver: int = SOLVER_PCG, push_apart: bool = False, learned_backoff: bool = False) -> Params:
     """Parameters of the dam-break workloads (reference parameter names in fsim.h)."""
     p = Params()
     p.transfer = transfer
@@ -196,6 +234,7 @@ def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: 
     p.mg_coarse_sweeps = mg_coarse_sweeps
     p.mg_cluster_sweeps = mg_cluster_sweeps
     p.grid_solver = grid_solver
+    p.learned_backoff = int(learned_backoff)
     return p
 
 
@@ -478,3 +517,94 @@ def obstacle(kind: int, pos, *, r: float = 0.0, size=(0, 0, 0), speed=(0, 0, 0),
     o.spawn_speed = spawn_speed
     o.last_spawn_fraction = frac
     return o
+
+
+# ---------------------------------------------------------------- renderer
+def default_render_params(**kw) -> RenderParams:
+    """The reference GUI's fluid-surface settings and lights (fsim_render_default_params),
+    with any field overridden by keyword."""
+    p = RenderParams()
+    load_library().fsim_render_default_params(C.byref(p))
+    for k, v in kw.items():
+        f = getattr(p, k)
+        if isinstance(f, C.Array):
+            for i, x in enumerate(v):
+                f[i] = x
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def camera(eye, yaw: float, pitch: float, fov: float = 40.0, aspect: float = 1.0, near: float = 0.5,
+           far: float = 300.0) -> Camera:
+    """Camera3D-style camera: eye position, yaw / pitch in degrees (fsim_render_camera)."""
+    c = Camera()
+    e = (C.c_double * 3)(*eye)
+    load_library().fsim_render_camera(C.byref(c), e, yaw, pitch, fov, aspect, near, far)
+    return c
+
+
+def look_at_angles(eye, target):
+    """(yaw, pitch) in degrees of Camera3D's front vector from eye towards target."""
+    d = np.asarray(target, np.float64) - np.asarray(eye, np.float64)
+    d /= np.linalg.norm(d)
+    return float(np.degrees(np.arctan2(d[2], d[0]))), float(np.degrees(np.arcsin(d[1])))
+
+
+class Renderer:
+    """Headless screen-space fluid renderer (include/fsim_render.h)."""
+
+    def __init__(self, width: int, height: int):
+        self.lib = load_library()
+        self.width, self.height = width, height
+        self.r = C.c_void_p()
+        rc = self.lib.fsim_render_create(width, height, C.byref(self.r))
+        if rc != 0:
+            raise FsimError(f"fsim_render_create failed: {ERRORS.get(rc, rc)}")
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            raise FsimError(f"{what} failed: {ERRORS.get(rc, rc)}: {self.lib.fsim_render_last_error(self.r).decode()}")
+
+    def close(self):
+        if self.r:
+            self.lib.fsim_render_destroy(self.r)
+            self.r = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def frame(self, particles, cam: Camera, params: RenderParams, scene_depth=None):
+        """particles: (n, 5) float32 (pos, |v|, density) on the host, or a CUDA tensor of that shape."""
+        sd = None
+        if scene_depth is not None:
+            sd = C.c_void_p(scene_depth.data_ptr())
+        if hasattr(particles, "data_ptr"):
+            n = particles.shape[0]
+            self._check(self.lib.fsim_render_frame(self.r, C.c_void_p(particles.data_ptr()), n, DEVICE,
+                                                   C.byref(cam), C.byref(params), sd, None), "fsim_render_frame")
+        else:
+            pts = np.ascontiguousarray(particles, np.float32).reshape(-1, 5)
+            self._keep = pts
+            self._check(self.lib.fsim_render_frame(self.r, _ptr(pts) if pts.size else None, pts.shape[0], HOST,
+                                                   C.byref(cam), C.byref(params), sd, None), "fsim_render_frame")
+
+    def frame_sim(self, sim: "Simulation", cam: Camera, params: RenderParams, scene_depth=None):
+        """Render a simulation context's particles (fsim_render_ctx; no host round trip)."""
+        sd = None if scene_depth is None else C.c_void_p(scene_depth.data_ptr())
+        self._check(self.lib.fsim_render_ctx(self.r, sim.ctx, C.byref(cam), C.byref(params), sd), "fsim_render_ctx")
+
+    def read(self, image: int = IMG_COLOR) -> np.ndarray:
+        four = image in (IMG_COLOR, IMG_NORMAL_DEPTH)
+        out = np.empty((self.height, self.width, 4) if four else (self.height, self.width), np.float32)
+        self._check(self.lib.fsim_render_read(self.r, image, _ptr(out), HOST), "fsim_render_read")
+        return out
+
+    def stats(self):
+        ms = C.c_float()
+        n = C.c_int()
+        self._check(self.lib.fsim_render_stats(self.r, C.byref(ms), C.byref(n)), "fsim_render_stats")
+        return ms.value, n.value

@@ -172,7 +172,10 @@ typedef struct fsim_params {
     int mg_coarse_sweeps;   /* the same on level 1 and other levels run as separate kernels (0: 6) */
     int mg_cluster_sweeps;  /* the same on the small levels run by one thread-block cluster (0: 6) */
     int grid_solver;        /* fsim_grid_solver: SimulationConfig::gridSolverType */
-    int reserved[2];
+    int learned_backoff;    /* FSIM_WARM_LEARNED: after a rejected network guess skip the network on
+                               the next 1, 2, 4 ... 64 solves (previous pressure instead); 0: judge
+                               the network on every solve */
+    int reserved[1];
 } fsim_params;
 
 /* Obstacle (obstacles.hpp:7-65), speed set by the caller as (pos-prevPos)/dt. */

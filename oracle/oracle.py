@@ -276,3 +276,32 @@ def obstacle(kind: int, pos, *, r: float = 0.0, size=(0, 0, 0), speed=(0, 0, 0),
     o.spawn_speed = spawn_speed
     o.last_spawn_fraction = frac
     return o
+
+
+# ---------------------------------------------------------------- renderer
+def render_frame(particles, camera, params, width: int, height: int, scene_depth=None):
+    """The CPU restatement of the reference's fluid shaders (render_oracle.c).
+
+    particles: (n, 5) float32 records (pos xyz, |v|, density) in the layout of
+    fsim_particle_gfx; camera / params: ctypes structures laid out as
+    fsim_camera / fsim_render_params.  Returns a dict of images (row 0 at the
+    bottom): raw_depth, depth, thickness (H, W) and normal_depth, color (H, W, 4).
+    """
+    lib = _load(PORT_LIB)
+    fn = lib.render_oracle_frame
+    fn.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    fn.restype = C.c_int
+    pts = np.ascontiguousarray(particles, np.float32).reshape(-1, 5)
+    out = {"raw_depth": np.empty((height, width), np.float32), "depth": np.empty((height, width), np.float32),
+           "thickness": np.empty((height, width), np.float32),
+           "normal_depth": np.empty((height, width, 4), np.float32),
+           "color": np.empty((height, width, 4), np.float32)}
+    sc = None if scene_depth is None else np.ascontiguousarray(scene_depth, np.float32)
+    rc = fn(pts.ctypes.data if pts.size else None, pts.shape[0], C.addressof(camera), C.addressof(params),
+            None if sc is None else sc.ctypes.data, width, height, out["raw_depth"].ctypes.data,
+            out["depth"].ctypes.data, out["thickness"].ctypes.data, out["normal_depth"].ctypes.data,
+            out["color"].ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"render_oracle_frame failed: {rc}")
+    return out

@@ -236,3 +236,29 @@ def test_training_and_learned_guess_gain(gpu):
     assert sum(its_learned) < sum(its_zero)
     solver.sim.set_net(None)
     net.close()
+
+
+@pytest.mark.gpu
+def test_learned_backoff_skips_a_losing_network(gpu):
+    """The untrained network predicts the zero guess, which never beats the previous
+    pressure (also zero here): with learned_backoff the network runs on solves
+    1, 3, 6 (back-off 1, then 2) and is skipped in between."""
+    from fluid_simulator_gb300 import native as N
+    from fluid_simulator_gb300 import warmstart as W
+    n = 32
+    solver = W.ProblemSolver(n)
+    net = N.WarmStartNet(seed=1)
+    solver.sim.set_net(net)
+    flags, rhs = W.make_problem(n, 5)
+    ran, used = [], []
+    for _ in range(6):
+        _, s = solver.solve(flags, rhs, warm=N.WARM_LEARNED, tol=1e-6, backoff=True)
+        ran.append(s.ms_guess > 0)
+        used.append(s.guess_used)
+    assert ran == [True, False, True, False, False, True]
+    assert all(u == N.WARM_PREVIOUS for u in used)
+    # without back-off the network is judged every time
+    _, s = solver.solve(flags, rhs, warm=N.WARM_LEARNED, tol=1e-6, backoff=False)
+    assert s.ms_guess > 0
+    solver.sim.set_net(None)
+    net.close()
