@@ -216,7 +216,8 @@ def run_fsim(args):
     p = N.default_params(transfer=N.APIC, resolution=res, tol=1e-6, tol_mode=N.TOL_REL_L2, max_iters=2000,
                          spawning=True, despawning=True, timing=True, precision=N.PREC_MIXED,
                          warm_start=N.WARM_ZERO, precond=precond, mg_sweeps=args.mg_sweeps,
-                         mg_coarse_sweeps=args.mg_coarse_sweeps, mg_cluster_sweeps=args.mg_cluster_sweeps)
+                         mg_coarse_sweeps=args.mg_coarse_sweeps, mg_cluster_sweeps=args.mg_cluster_sweeps,
+                         refine_digits=args.refine_digits)
     sim = N.Simulation(res, p)
     sim.set_particles(pos)
     del pos
@@ -317,6 +318,7 @@ def run_fsim(args):
                    "warm_start": "zero", "precond": args.precond},
         "particle_steps_per_s": round(np_mean * value, 1),
         "pcg_iterations_mean": round(its, 2),
+        "pcg_refinements_mean": round(mean("reliable_updates"), 2),
         "stage_ms": {k: round(mean(k), 3) for k in ("ms_simulate_particles", "ms_p2g", "ms_p2g_kernel", "ms_prep",
                                                    "ms_pcg_setup", "ms_solve", "ms_extrapolate", "ms_g2p")},
         "pcg_ms_per_iteration": round(pcg_ms_per_it, 4),
@@ -341,11 +343,56 @@ def run_fsim(args):
         line["pcg_precision"] = precision_study(sim, dt, N)
     if args.ws_steps > 0:
         line["pcg_warm_start"] = warm_start_study(sim, dt, t, h, N, args)
+    if args.render:
+        line["render"] = render_study(sim, N, h, peak)
     sim.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(res, dt)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- renderer
+def render_study(sim, N, h, peak):
+    """One 1000 x 1000 frame of the simulation's particles through the headless
+    renderer (fsim_render_ctx: gfx publish + every FluidSurfaceGfx pass), with the
+    reference GUI's settings scaled from its 40-unit box to the unit box."""
+    W = H = 1000
+    r = N.Renderer(W, H)
+    eye = (1.9, 1.3, 2.3)
+    yaw, pitch = N.look_at_angles(eye, (0.5, 0.3, 0.5))
+    cam = N.camera(eye, yaw, pitch, fov=40.0, aspect=1.0, near=0.05, far=20.0)
+    s = 1.0 / 40.0
+    prm = N.default_render_params(particle_radius=h / 4, smoothing_size=2.4 * s, transparency_blur_size=2.4 * s,
+                                  noise_scale=0.956 / s)
+    for l in range(prm.num_lights):
+        for k in range(3):
+            prm.lights[l].position[k] *= s
+            prm.lights[l].power_density[k] *= s * s
+    for _ in range(2):
+        r.frame_sim(sim, cam, prm)
+    sim.synchronize()
+    frames, kernel_ms = 5, []
+    t0 = time.perf_counter()
+    for f in range(frames):
+        prm.noise_offset = 0.317 * 10.0 * f / 60.0
+        r.frame_sim(sim, cam, prm)
+        ms, launches = r.stats()
+        kernel_ms.append(ms)
+    sim.synchronize()
+    wall_ms = (time.perf_counter() - t0) * 1e3 / frames
+    n = sim.n
+    covered = int((r.read(N.IMG_RAW_DEPTH) < 1.0).sum())
+    r.close()
+    # algorithmic bytes: three particle passes over the 20-byte records (surface
+    # splat, spray splat, thickness splat) + the image passes (~120 B per pixel)
+    alg = 3 * 20 * n + 120 * W * H
+    k = statistics.median(kernel_ms)
+    return {"image": [W, H], "particles": n, "covered_pixels": covered, "ms_per_frame_kernels": round(k, 3),
+            "ms_per_frame_wall": round(wall_ms, 3), "launches_per_frame": launches,
+            "algorithmic_bytes": alg, "achieved_gbs": round(alg / (k / 1e3) / 1e9, 1),
+            "frac": round(alg / (k / 1e3) / 1e9 / peak, 4),
+            "note": "wall time includes fsim_fill_gfx (device) and the Python call"}
 
 
 # ---------------------------------------------------------------- precision study
@@ -546,9 +593,12 @@ def main():
                     help="multigrid sweeps on the levels run by the cluster kernel (0: library default)")
     ap.add_argument("--precision-study", type=int, default=1,
                     help="solve the last step's pressure problem in FP64 / mixed / FP32 and report errors (0: skip)")
-    ap.add_argument("--ws-steps", type=int, default=4,
+    ap.add_argument("--ws-steps", type=int, default=8,
                     help="problems of the zero / previous / learned warm-start comparison (0: skip)")
     ap.add_argument("--ws-problems", type=int, default=48, help="synthetic training problems at 64^3")
+    ap.add_argument("--render", type=int, default=1, help="time one 1000x1000 frame of the headless renderer")
+    ap.add_argument("--refine-digits", type=int, default=0,
+                    help="mixed-precision refinement every 10^k residual drop (0: library default 3)")
     ap.add_argument("--ws-iters", type=int, default=600, help="Adam iterations of the warm-start network")
     args = ap.parse_args()
     os.makedirs(args.out_dir, exist_ok=True)

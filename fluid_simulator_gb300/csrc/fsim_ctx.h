@@ -17,6 +17,7 @@ struct PcgState {
     double alpha, beta;
     double rmax, rr;     // recursive residual max |r|, r.r   (A' units)
     double rr_update;    // r.r right after the last true-residual replacement
+    double fold_drop;    // MIXED: fold + restart once r.r < fold_drop * rr_update
     double bb, bmax;     // rhs norms (A' units)
     double tol_abs;      // max-norm tolerance in A' units
     double tol_rel2;     // (tol * ||b||)^2 in A' units
@@ -28,7 +29,7 @@ struct PcgState {
     int nan;
     int skip;            // rhs below the reference's early-out (sum b^2 < 1e-7)
     int bufsel;          // bit 0: current r buffer, bit 1: current s buffer
-    int fold_enabled;    // MIXED: stop the inner iteration when the residual fell 100x
+    int fold_enabled;    // MIXED: stop the inner iteration when r.r fell by fold_drop
     int need_fold;       // set by the iteration when a fold + restart is due
     int guess_used;      // the judged guess had the smaller residual and seeds PCG
 };
@@ -45,6 +46,7 @@ struct MGLevelBufs {
 };
 
 struct SolverBufs {
+    double conv_rate = 0.0;    // measured PCG residual-norm factor per iteration (chunk planning)
     int nbx, nby, nbz;         // bricks per axis
     long long nbricks;
     int* brick_list = nullptr; // active bricks (contain a fluid cell), ascending

@@ -483,9 +483,9 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
             st->converged = conv ? 1 : 0;
             if (conv || st->it >= st->max_iters || !isfinite(acc[0])) st->done = 1;
             if (!isfinite(acc[0])) st->nan = 1;
-            // the FP32 recursion is trusted for a 100x residual drop, then the
+            // the FP32 recursion is trusted for a fold_drop fall of r.r, then the
             // solution is folded into FP64 and the iteration restarts
-            if (st->fold_enabled && acc[0] < 0.01 * st->rr_update) {
+            if (st->fold_enabled && acc[0] < st->fold_drop * st->rr_update) {
                 st->need_fold = 1;
                 st->done = 1;
             }
@@ -510,6 +510,13 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
 // (2, 2, 2) took 30 iterations at 0.83 ms, (3, 6, 6) 16 iterations at 1.30 ms.
 // The coarse correction near the free surface is the weak part of the cycle,
 // so extra coarse smoothing pays for itself.
+// MIXED precision: the FP32 recursion is folded into the FP64 solution (true
+// FP64 residual, CG restart) each time the residual norm fell this many decades.
+// The FP32 correction restarts from zero at every fold, so the drift between the
+// recursive and the true residual stays near FP32 rounding of the fold's
+// residual, far below a 10^-3 drop.  One decade per fold (the first setting)
+// cost 5 refinements per 1e-6 solve at 256^3.
+constexpr int MIXED_REFINE_DIGITS = 3;
 constexpr int MG_NU_DEFAULT = 3;           // level 0
 constexpr int MG_NU_COARSE_DEFAULT = 6;    // level 1 and other separately launched levels
 constexpr int MG_NU_CLUSTER_DEFAULT = 6;   // levels run by the cluster kernel
@@ -973,7 +980,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update_q(const PcgArgs a, Vecs<
             st->converged = conv ? 1 : 0;
             if (conv || st->it >= st->max_iters || !isfinite(acc[0])) st->done = 1;
             if (!isfinite(acc[0])) st->nan = 1;
-            if (st->fold_enabled && acc[0] < 0.01 * st->rr_update) {
+            if (st->fold_enabled && acc[0] < st->fold_drop * st->rr_update) {
                 st->need_fold = 1;
                 st->done = 1;
             }
@@ -1679,17 +1686,45 @@ static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, int prec
         S.iter_kernels = (int)(ctx->launches - l0);
         ctx->launches = l0;
     }
-    int chunk = mg ? 2 : 4;
-    const int chunk_max = mg ? 8 : 16;
+    // Iterations are launched in chunks between host reads of the state.  The
+    // chunk is the number of iterations the measured convergence rate (residual
+    // norm factor per iteration, carried over from earlier solves) needs to reach
+    // the next stop -- the tolerance or the next fold -- so that few iterations
+    // are launched past the stop (they exit at once) and few reads are wasted.
+    const int chunk_cap = mg ? 16 : 64;
+    auto plan = [&]() -> int {
+        const PcgState& h = *S.st_host;
+        const double rate = S.conv_rate;
+        if (!(rate > 0.0 && rate < 1.0)) return mg ? 2 : 4;
+        const double lr = std::log(rate);
+        double n = 1e9;
+        if (h.tol_mode == FSIM_TOL_ABS_MAX) {
+            if (h.rmax > 0.0 && h.tol_abs > 0.0) n = std::log(h.tol_abs / h.rmax) / lr;
+        } else if (h.rr > 0.0 && h.tol_rel2 > 0.0) {
+            n = 0.5 * std::log(h.tol_rel2 / h.rr) / lr;
+        }
+        if (fold && h.rr > 0.0 && h.rr_update > 0.0)
+            n = std::min(n, 0.5 * std::log(h.fold_drop * h.rr_update / h.rr) / lr);
+        return (int)std::min<double>(chunk_cap, std::max(1.0, std::ceil(n)));
+    };
+    int chunk = plan();
+    int it_mark = S.st_host->it;
+    double rr_mark = S.st_host->rr;
     while (!S.st_host->done && !S.st_host->nan) {
         for (int k = 0; k < chunk; k++) {
             FSIM_CUDA_TRY(ctx, cudaGraphLaunch(S.iter_exec, st));
             ctx->launches += S.iter_kernels;
         }
         if ((rc = read_state())) return rc;
-        if (chunk < chunk_max) chunk *= 2;
         PcgState& h = *S.st_host;
         if (h.nan) break;
+        if (h.it > it_mark && rr_mark > 0.0 && h.rr > 0.0 && h.rr < rr_mark) {
+            const double r = std::pow(h.rr / rr_mark, 0.5 / (h.it - it_mark));
+            S.conv_rate = S.conv_rate > 0.0 ? 0.5 * (S.conv_rate + r) : r;
+        }
+        it_mark = h.it;
+        rr_mark = h.rr;
+        chunk = plan();
         const bool need_fold = fold && (h.need_fold || h.done);
         if (need_fold && !h.skip) {
             // fold the FP32 correction into the FP64 solution, recompute the true
@@ -1707,7 +1742,9 @@ static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, int prec
             if ((rc = read_state())) return rc;
             if (!h.done && it_before >= h.max_iters) h.done = 1;
             if (h.done) break;
-            chunk = mg ? 2 : 4;
+            it_mark = h.it;
+            rr_mark = h.rr;
+            chunk = plan();
         } else if (h.done) {
             break;
         }
@@ -1785,6 +1822,10 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     h.max_iters = max_iters;
     h.tol_abs = tol / scale;
     h.fold_enabled = (precision == FSIM_PREC_MIXED) ? 1 : 0;
+    {
+        const int d = ctx->prm.refine_digits > 0 ? std::min(ctx->prm.refine_digits, 6) : MIXED_REFINE_DIGITS;
+        h.fold_drop = std::pow(10.0, -2.0 * d);  // on r.r
+    }
     *S.st_host = h;
     FSIM_CUDA_TRY(ctx, cudaMemcpyAsync(S.st, S.st_host, sizeof(PcgState), cudaMemcpyHostToDevice, st));
 

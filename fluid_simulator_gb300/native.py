@@ -48,7 +48,7 @@ class Params(C.Structure):
         ("tol_mode", C.c_int), ("particle_r", C.c_double), ("precision", C.c_int),
         ("warm_start", C.c_int), ("track_ids", C.c_int), ("timing", C.c_int), ("precond", C.c_int),
         ("mg_sweeps", C.c_int), ("mg_coarse_sweeps", C.c_int), ("mg_cluster_sweeps", C.c_int),
-        ("grid_solver", C.c_int), ("learned_backoff", C.c_int), ("reserved", C.c_int * 1),
+        ("grid_solver", C.c_int), ("learned_backoff", C.c_int), ("refine_digits", C.c_int),
     ]
 
 
@@ -204,7 +204,8 @@ def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: 
                    pressure_enabled: bool = False, pressure_k: float = 2.0, average_pressure: float = 2.0,
                    fluid_density: float = 1.0, timing: bool = False, precond: int = PRECOND_MG,
                    mg_sweeps: int = 0, mg_coarse_sweeps: int = 0, mg_cluster_sweeps: int = 0,
-                   grid_solver: int = SOLVER_PCG, push_apart: bool = False, learned_backoff: bool = False) -> Params:
+                   grid_solver: int = SOLVER_PCG, push_apart: bool = False, learned_backoff: bool = False,
+                   refine_digits: int = 0) -> Params:
     """Parameters of the dam-break workloads (reference parameter names in fsim.h)."""
     p = Params()
     p.transfer = transfer
@@ -235,6 +236,7 @@ def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: 
     p.mg_cluster_sweeps = mg_cluster_sweeps
     p.grid_solver = grid_solver
     p.learned_backoff = int(learned_backoff)
+    p.refine_digits = refine_digits
     return p
 
 

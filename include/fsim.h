@@ -175,7 +175,9 @@ typedef struct fsim_params {
     int learned_backoff;    /* FSIM_WARM_LEARNED: after a rejected network guess skip the network on
                                the next 1, 2, 4 ... 64 solves (previous pressure instead); 0: judge
                                the network on every solve */
-    int reserved[1];
+    int refine_digits;      /* FSIM_PREC_MIXED: fold the FP32 correction into the FP64 pressure and
+                               restart from the true FP64 residual each time the residual norm fell
+                               10^refine_digits (0: 3) */
 } fsim_params;
 
 /* Obstacle (obstacles.hpp:7-65), speed set by the caller as (pos-prevPos)/dt. */
