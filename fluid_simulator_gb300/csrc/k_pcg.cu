@@ -506,10 +506,12 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
 // correction and black->red after it; the coarsest level (<= 512 cells) is
 // smoothed BOTTOM times each way inside one CTA.  Starting every level from
 // zero, the V-cycle is a fixed symmetric linear operator, as CG requires.
-// Sweeps per level group, measured on the 256^3 fill workload (PCG to 1e-6):
-// (2, 2, 2) took 30 iterations at 0.83 ms, (3, 6, 6) 16 iterations at 1.30 ms.
-// The coarse correction near the free surface is the weak part of the cycle,
-// so extra coarse smoothing pays for itself.
+// Sweeps per level group, measured on the 256^3 fill workload (PCG to 1e-6,
+// steps/s of the whole step): (2, 2, 2) took 30 iterations; (3, 6, 6) 16.3
+// iterations, 34.0 steps/s; (2, 6, 6) 17 iterations, 35.4; (1, 6, 6) 18.8, 35.8;
+// (2, 4, 6) 17.8, 35.3.  A fine-level sweep costs ~107 us in place, a level-1
+// sweep ~22 us: the coarse correction near the free surface is the weak part of
+// the cycle, so coarse smoothing pays for itself and fine smoothing does not.
 // MIXED precision: the FP32 recursion is folded into the FP64 solution (true
 // FP64 residual, CG restart) each time the residual norm fell this many decades.
 // The FP32 correction restarts from zero at every fold, so the drift between the
@@ -517,7 +519,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
 // residual, far below a 10^-3 drop.  One decade per fold (the first setting)
 // cost 5 refinements per 1e-6 solve at 256^3.
 constexpr int MIXED_REFINE_DIGITS = 3;
-constexpr int MG_NU_DEFAULT = 3;           // level 0
+constexpr int MG_NU_DEFAULT = 2;           // level 0
 constexpr int MG_NU_COARSE_DEFAULT = 6;    // level 1 and other separately launched levels
 constexpr int MG_NU_CLUSTER_DEFAULT = 6;   // levels run by the cluster kernel
 constexpr int MG_BOTTOM_SWEEPS = 12;
@@ -1039,7 +1041,11 @@ __global__ void __launch_bounds__(1024) k_mg_bottom(const PcgState* st, MGLev L)
 // level of latency-bound small kernels.
 constexpr int MG_MAX_LEVELS = 12;
 constexpr int MG_CLUSTER_THREADS = 1024;
-constexpr long long MG_CLUSTER_CELLS = 300000;  // largest level handed to the cluster kernel
+// Largest level handed to the cluster kernel.  At 256^3 the 64^3 level (262k
+// cells) ran ~8 us per pass on the cluster's 16 SMs and is faster as separate
+// full-GPU launches (35.6 -> 37.5 steps/s); moving the 32^3 level out as well
+// changed nothing.
+constexpr long long MG_CLUSTER_CELLS = 40000;
 
 struct MGChain {
     MGLev lev[MG_MAX_LEVELS];

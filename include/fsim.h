@@ -168,7 +168,7 @@ typedef struct fsim_params {
     int timing;             /* record per-stage CUDA-event times into fsim_step_stats */
     int precond;            /* fsim_precond (FSIM_PREC_FP64 always uses FSIM_PRECOND_RBIC) */
     int mg_sweeps;          /* multigrid smoothing sweeps before and after the coarse correction on
-                               the finest level (0: 3) */
+                               the finest level (0: 2) */
     int mg_coarse_sweeps;   /* the same on level 1 and other levels run as separate kernels (0: 6) */
     int mg_cluster_sweeps;  /* the same on the small levels run by one thread-block cluster (0: 6) */
     int grid_solver;        /* fsim_grid_solver: SimulationConfig::gridSolverType */
