@@ -247,26 +247,40 @@ def run_fsim(args):
     ms_max = dist_max(dist, ms)
     clocks = clk.summary()
 
-    # end to end through the C ABI with the renderer hand-off in pinned host memory
+    # end to end through the C ABI with the renderer hand-off in pinned host memory:
+    # each step's records are published asynchronously (fsim_fill_gfx_async) and
+    # land in host memory while the next step runs; the timed region ends after
+    # the last copy (fsim_gfx_wait)
     n_cap = int(sim.n * 1.2) + 1_000_000
     gfx = (N.ParticleGfx * n_cap)()
     rt.cudaHostRegister(C.cast(gfx, C.c_void_p), C.c_size_t(C.sizeof(gfx)), 0)
     e2e_steps = max(1, min(args.steps, 5))
     d2h = 0
     h2d = 0
-    barrier(dist)
-    ev.start()
-    for _ in range(e2e_steps):
+
+    def e2e_step():
+        nonlocal t, d2h, h2d
         obs = obstacles_at(t, dt, h, N)
         h2d += len(obs) * C.sizeof(N.Obstacle)
         sim.set_obstacles(obs)
         sim.step(dt)
         t += dt
         got = C.c_int64()
-        rc = sim.lib.fsim_fill_gfx(sim.ctx, gfx, n_cap, C.byref(got), N.HOST)
-        if rc != 0:
-            raise RuntimeError("fsim_fill_gfx failed")
+        if sim.lib.fsim_fill_gfx_async(sim.ctx, gfx, n_cap, C.byref(got)) != 0:
+            raise RuntimeError("fsim_fill_gfx_async failed")
         d2h += got.value * C.sizeof(N.ParticleGfx)
+
+    # one untimed warm-up step per staging slot (their one-time allocation)
+    for _ in range(2):
+        e2e_step()
+    sim.lib.fsim_gfx_wait(sim.ctx)
+    d2h = h2d = 0
+    barrier(dist)
+    ev.start()
+    for _ in range(e2e_steps):
+        e2e_step()
+    if sim.lib.fsim_gfx_wait(sim.ctx) != 0:
+        raise RuntimeError("fsim_gfx_wait failed")
     e2e_ms = ev.stop_ms()
     barrier(dist)
     e2e_ms = dist_max(dist, e2e_ms)
@@ -336,7 +350,8 @@ def run_fsim(args):
         "clocks": clocks,
         "e2e": {"value": round(world * e2e_steps / (e2e_ms / 1000.0), 4), "unit": "steps/s",
                 "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps,
-                "steps": e2e_steps, "path": "fsim_step + fsim_fill_gfx(pinned host) per step"},
+                "steps": e2e_steps,
+                "path": "fsim_set_obstacles + fsim_step + fsim_fill_gfx_async(pinned host) per step, fsim_gfx_wait"},
         "gpu_launches": int(sum(s.kernel_launches for s in stats)),
     }
     if args.precision_study:

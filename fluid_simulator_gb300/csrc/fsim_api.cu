@@ -208,7 +208,8 @@ int sort_by_cell(fsim_ctx* ctx) {
     launch_scan(ctx->count, ctx->cstart, ctx->g.ncell, ctx->scan_blocks, ctx->stream);
     launch_scatter(ctx->key, ctx->rank, ctx->cstart, ctx->perm, ctx->n, ctx->stream);
     ctx->launches += 3 + (ctx->n > 0 ? 1 : 0);
-    cudaMemcpyAsync(ctx->h_misc, ctx->cstart + ctx->g.ncell, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    fetch_small(ctx->h_misc, ctx->cstart + ctx->g.ncell, sizeof(int), ctx->stream);
+    ctx->launches += 1;
     CHECK_LAUNCH(ctx);
     ctx->sorted = true;
     return FSIM_OK;
@@ -342,8 +343,10 @@ int do_spawn(fsim_ctx* ctx, double dt) {
 }
 
 int check_device_error(fsim_ctx* ctx) {
-    unsigned e = 0;
-    FSIM_CUDA_TRY(ctx, cudaMemcpy(&e, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    unsigned* he = reinterpret_cast<unsigned*>(&ctx->h_misc[2]);
+    fetch_small(he, ctx->d_err, sizeof(unsigned), ctx->stream);
+    FSIM_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    const unsigned e = *he;
     if (e & FSIM_DERR_TMA_TIMEOUT) {
         cudaMemset(ctx->d_err, 0, sizeof(unsigned));
         return set_error(ctx, FSIM_E_TIMEOUT, "G2P tile load wait timed out");
@@ -459,6 +462,15 @@ int fsim_create(const fsim_grid_desc* gd, const fsim_params* params, fsim_ctx** 
 int fsim_destroy(fsim_ctx* ctx) {
     if (!ctx) return FSIM_OK;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        for (int k = 0; k < 2; k++) {
+            cudaFree(ctx->gfx_stage[k]);
+            if (ctx->gfx_ready[k]) cudaEventDestroy(ctx->gfx_ready[k]);
+            if (ctx->gfx_done[k]) cudaEventDestroy(ctx->gfx_done[k]);
+        }
+        cudaStreamDestroy(ctx->copy_stream);
+    }
     cudaFree(ctx->buf_mem[0]);
     cudaFree(ctx->buf_mem[1]);
     cudaFree(ctx->key); cudaFree(ctx->rank); cudaFree(ctx->perm);
@@ -874,6 +886,53 @@ int fsim_set_grid(fsim_ctx* ctx, int field, const void* in, int where) {
     CHECK_LAUNCH(ctx);
     if (tmp) FSIM_CUDA_TRY(ctx, cudaFreeAsync(tmp, s));
     FSIM_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return FSIM_OK;
+}
+
+int fsim_fill_gfx_async(fsim_ctx* ctx, fsim_particle_gfx* out, int64_t cap, int64_t* n_out) {
+    if (!ctx) return FSIM_E_INVALID;
+    const long long n = ctx->n;
+    if (n_out) *n_out = n;
+    if (n == 0 || !out) return FSIM_OK;
+    if (cap < n) return set_error(ctx, FSIM_E_INVALID, "output capacity below particle count");
+    if (!ctx->copy_stream) {
+        FSIM_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; k++) {
+            FSIM_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->gfx_ready[k], cudaEventDisableTiming));
+            FSIM_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->gfx_done[k], cudaEventDisableTiming));
+            FSIM_CUDA_TRY(ctx, cudaEventRecord(ctx->gfx_done[k], ctx->copy_stream));
+        }
+    }
+    const int k = ctx->gfx_slot;
+    // the copy out of this slot (two hand-offs ago) must finish before it is rewritten
+    FSIM_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->gfx_done[k], 0));
+    if (ctx->gfx_cap[k] < n) {
+        FSIM_CUDA_TRY(ctx, cudaEventSynchronize(ctx->gfx_done[k]));
+        cudaFree(ctx->gfx_stage[k]);
+        ctx->gfx_stage[k] = nullptr;
+        ctx->gfx_cap[k] = 0;
+        const long long c = n + n / 8 + 4096;
+        if (cudaMalloc(&ctx->gfx_stage[k], (size_t)c * sizeof(fsim_particle_gfx)) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(ctx, FSIM_E_OOM, "gfx staging buffer");
+        }
+        ctx->gfx_cap[k] = c;
+    }
+    launch_gfx(ctx->buf[ctx->cur], n, ctx->avg, ctx->g, ctx->gfx_stage[k], ctx->stream);
+    ctx->launches += 1;
+    CHECK_LAUNCH(ctx);
+    FSIM_CUDA_TRY(ctx, cudaEventRecord(ctx->gfx_ready[k], ctx->stream));
+    FSIM_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->gfx_ready[k], 0));
+    FSIM_CUDA_TRY(ctx, cudaMemcpyAsync(out, ctx->gfx_stage[k], (size_t)n * sizeof(fsim_particle_gfx),
+                                       cudaMemcpyDeviceToHost, ctx->copy_stream));
+    FSIM_CUDA_TRY(ctx, cudaEventRecord(ctx->gfx_done[k], ctx->copy_stream));
+    ctx->gfx_slot = 1 - k;
+    return FSIM_OK;
+}
+
+int fsim_gfx_wait(fsim_ctx* ctx) {
+    if (!ctx) return FSIM_E_INVALID;
+    if (ctx->copy_stream) FSIM_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->copy_stream));
     return FSIM_OK;
 }
 

@@ -78,6 +78,14 @@ struct fsim_ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    // asynchronous gfx hand-off (fsim_fill_gfx_async): double-buffered device
+    // staging, copied to the host on copy_stream
+    cudaStream_t copy_stream = nullptr;
+    fsim_particle_gfx* gfx_stage[2] = {nullptr, nullptr};
+    long long gfx_cap[2] = {0, 0};
+    cudaEvent_t gfx_ready[2] = {nullptr, nullptr};
+    cudaEvent_t gfx_done[2] = {nullptr, nullptr};
+    int gfx_slot = 0;
     fsim_params prm{};
     GridGeom g{};
     std::string err;
@@ -159,6 +167,12 @@ void launch_spawn_disc(ParticleBuf p, long long first, int ncells, const fsim_ob
                        uint32_t first_id, bool ids, cudaStream_t s);
 void launch_push_apart(ParticleBuf p, const uint32_t* perm, const int* cstart, const GridGeom& g, long long n,
                        double r, const float lo[3], const float hi[3], float* const out[3], cudaStream_t s);
+// Small device -> pinned-host reads (solver state, counts, error flags) by a
+// one-warp kernel writing through the host mapping instead of a DMA copy, so
+// that they never queue behind a large copy-engine transfer (the asynchronous
+// gfx hand-off).  `host` must be cudaMallocHost memory; valid after a
+// synchronize of `s`.
+void fetch_small(void* host, const void* dev, int bytes, cudaStream_t s);
 void launch_gfx(ParticleBuf p, long long n, const float* avg, const GridGeom& g,
                 fsim_particle_gfx* out, cudaStream_t s);
 

@@ -313,6 +313,18 @@ int launch_obstacle(fsim_ctx* ctx, const fsim_obstacle& ob) {
     return 2;
 }
 
+namespace {
+__global__ void k_fetch_small(unsigned* dst, const unsigned* src, int words) {
+    for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+    __threadfence_system();
+}
+}  // namespace
+
+void fetch_small(void* host, const void* dev, int bytes, cudaStream_t s) {
+    // every caller's buffers are 4-byte aligned and a whole number of words
+    k_fetch_small<<<1, 32, 0, s>>>(static_cast<unsigned*>(host), static_cast<const unsigned*>(dev), (bytes + 3) / 4);
+}
+
 void launch_prep(fsim_ctx* ctx, int walls, int post, float gravity_inc) {
     const GridGeom& g = ctx->g;
     ctx->launches += 1;

@@ -1631,7 +1631,7 @@ static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, int prec
     const bool mg = (precond == FSIM_PRECOND_MG) && sizeof(T) == 4;
     int folds = 0;
     auto read_state = [&]() -> int {
-        FSIM_CUDA_TRY(ctx, cudaMemcpyAsync(S.st_host, S.st, sizeof(PcgState), cudaMemcpyDeviceToHost, st));
+        fetch_small(S.st_host, S.st, (int)sizeof(PcgState), st);
         FSIM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
         return FSIM_OK;
     };
@@ -1821,7 +1821,7 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     k_setup<<<ceil_div(g.ncell, 256), 256, 0, st>>>(sa);
     k_compact_bricks<<<1, 1024, 0, st>>>(S.brick_flag, S.nbricks, S.brick_list, S.d_nactive);
     ctx->launches += 2;
-    FSIM_CUDA_TRY(ctx, cudaMemcpyAsync(&ctx->h_misc[1], S.d_nactive, sizeof(int), cudaMemcpyDeviceToHost, st));
+    fetch_small(&ctx->h_misc[1], S.d_nactive, (int)sizeof(int), st);
 
     PcgState h{};
     h.tol_mode = tol_mode;

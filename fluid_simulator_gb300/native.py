@@ -110,6 +110,7 @@ EXPORTS = [
     "fsim_last_error", "fsim_stream", "fsim_synchronize", "fsim_set_particles", "fsim_add_particles",
     "fsim_get_particles", "fsim_num_particles", "fsim_set_obstacles", "fsim_get_obstacles",
     "fsim_step", "fsim_stage", "fsim_get_grid", "fsim_set_grid", "fsim_fill_gfx",
+    "fsim_fill_gfx_async", "fsim_gfx_wait",
     "fsim_set_pressure_guess", "fsim_solve_pressure", "fsim_solve_current", "fsim_p2g_noalloc",
     "fsim_net_create", "fsim_net_destroy", "fsim_net_last_error", "fsim_net_num_params",
     "fsim_net_get_params", "fsim_net_set_params", "fsim_net_forward", "fsim_net_backward",
@@ -151,6 +152,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "fsim_get_grid": (C.c_int, [P, C.c_int, P, C.c_int]),
         "fsim_set_grid": (C.c_int, [P, C.c_int, P, C.c_int]),
         "fsim_fill_gfx": (C.c_int, [P, C.POINTER(ParticleGfx), i64, C.POINTER(i64), C.c_int]),
+        "fsim_fill_gfx_async": (C.c_int, [P, C.POINTER(ParticleGfx), i64, C.POINTER(i64)]),
+        "fsim_gfx_wait": (C.c_int, [P]),
         "fsim_set_pressure_guess": (C.c_int, [P, fp, C.c_int]),
         "fsim_solve_pressure": (C.c_int, [P, dp, C.c_double, C.c_int, C.c_int, C.c_double, C.c_int, dp,
                                           C.POINTER(StepStats)]),

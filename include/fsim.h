@@ -287,6 +287,16 @@ int fsim_set_grid(fsim_ctx *ctx, int field, const void *in, int where);
 /* ---- renderer hand-off (SimulationManager::getParticleGfxData,
  *      simulationManager.cpp:218-231) ------------------------------------- */
 int fsim_fill_gfx(fsim_ctx *ctx, fsim_particle_gfx *out, int64_t cap, int64_t *n, int where);
+/* The same hand-off without waiting (simulationThreadWorker's publish overlapped
+ * with the following steps): the records are written into a device staging
+ * buffer on the context's stream and copied to the host buffer `out` on a
+ * separate copy stream; the call returns at once with *n.  Pinned or
+ * registered `out` gives DMA-engine speed.  Two hand-offs can be in flight
+ * (double-buffered staging); `out` must not be read or reused before
+ * fsim_gfx_wait returns. */
+int fsim_fill_gfx_async(fsim_ctx *ctx, fsim_particle_gfx *out, int64_t cap, int64_t *n);
+/* Blocks until every fsim_fill_gfx_async copy has landed in host memory. */
+int fsim_gfx_wait(fsim_ctx *ctx);
 
 /* ---- pressure warm start ----------------------------------------------- */
 /* Initial guess for the next solve (FP32, reference cell order); used when

@@ -302,3 +302,27 @@ def test_gfx_publish_matches_particles_and_density(gpu, pinned):
                 dens += w * avg[x, y, z]
     assert np.allclose(gfx[:, 4], dens, rtol=1e-4, atol=1e-5)
     sim.close()
+
+
+def test_async_gfx_handoff_equals_sync(gpu):
+    """fsim_fill_gfx_async over consecutive steps (both staging slots reused)
+    delivers exactly what fsim_fill_gfx gives for the same state."""
+    import ctypes as C
+
+    pos = dam_break(GridSpec(32), seed=4)
+    sim = N.Simulation(32, N.default_params(transfer=N.APIC, resolution=32))
+    sim.set_particles(pos)
+    n = sim.n
+    bufs = [(N.ParticleGfx * n)() for _ in range(3)]
+    want = []
+    for s in range(3):
+        sim.step(DT32)
+        want.append(sim.gfx())
+        got = C.c_int64()
+        assert sim.lib.fsim_fill_gfx_async(sim.ctx, bufs[s], n, C.byref(got)) == 0
+        assert got.value == n
+    assert sim.lib.fsim_gfx_wait(sim.ctx) == 0
+    for s in range(3):
+        arr = np.frombuffer(bufs[s], dtype=np.float32, count=5 * n).reshape(n, 5)
+        assert np.array_equal(arr, want[s])
+    sim.close()
