@@ -1,12 +1,13 @@
 // k_transfer.cu -- particle <-> grid transfers on cell-sorted particles.
 //
-// Both kernels work on tiles of TX x TY x TZ cells (one CTA per tile).
+// Both kernels work on tiles of cells (one CTA per tile): P2G on PX x PY x PZ,
+// G2P on TX x TY x TZ.
 //
 // P2G (Simulator::p2gTransfer, simulator.cpp:314-352, fused with
 // markFluidCellsAndCalculateParticleDensities, simulator.cpp:354-368): the CTA
 // owns the faces and cell centres of its tile and computes their final values,
 // so no grid accumulator ever goes to global memory and no global atomic is
-// used.  Each thread takes one cell of the tile plus its one-cell halo, walks
+// used.  Each lane takes one cell of the tile plus its one-cell halo, walks
 // that cell's particles (contiguous in the sorted order) and adds their
 // trilinear contributions to the tile's shared-memory accumulators; lanes of a
 // warp hold distinct cells, so their shared-memory adds do not collide.  The
@@ -43,11 +44,14 @@ struct P2GArgs {
     int ntx, nty, ntz;
 };
 
-// P2G tile (owned cells) and its one-cell halo
-constexpr int PX = 12, PY = 16, PZ = 32;
+// P2G tile (owned cells) and its one-cell halo: 12x16x16 owned cells, seven
+// FP32 shared accumulators per cell (face v and weight per axis, density) =
+// 86 KB, so two 384-thread CTAs fit on an SM
+constexpr int PX = 12, PY = 16, PZ = 16;
 constexpr int QX = PX + 2, QY = PY + 2, QZ = PZ + 2;
 constexpr int PCELLS = PX * PY * PZ;
-constexpr int P2G_SMEM_V2 = 7 * PCELLS * (int)sizeof(float);  // 172,032 B
+constexpr int P2G_SMEM = 7 * PCELLS * (int)sizeof(float);  // 86,016 B
+constexpr int P2G_THREADS = 384;
 
 // 1D tent weights of the three cell-centred nodes at relative -0.5, 0.5, 1.5
 // (f = position in the cell, 0 <= f < 1): the two nodes the reference's
@@ -58,26 +62,21 @@ __device__ __forceinline__ void tent3(float f, float (&w)[3]) {
     w[2] = fmaxf(0.f, f - 0.5f);
 }
 
-// Warps come in pairs over blocks of 32 consecutive tile+halo cells (one cell
-// per lane).  The even warp of a pair handles the x faces and the cell-centre
-// density of its cells, the odd warp the y and z faces; both walk the same
-// particles at the same time, so the second reads hit L1.  Each lane walks its
-// cell's particles once and accumulates, in registers, the full 2x3x3 face
-// stencil of its axes (faces of the cells at normal offset -1, 0 and
-// transverse offsets -1, 0, +1: the union of getFacesAround's 8-face stencils
-// over the cell) and the 3x3x3 stencil of getCellsAround -- the merged
-// contribution of all particles of the cell.  It then adds the entries inside
-// the tile to the tile's shared accumulators (lanes hold distinct cells, so a
-// warp's adds never collide).
-constexpr int P2G_THREADS_V2 = 384;
-
-// accumulators of one lane: role 0 uses [0,18) weights x, [18,36) values x,
-// [36,63) density; role 1 uses [0,18)/[18,36) for y and [36,54)/[54,72) for z
-constexpr int NACC = 72;
-
-template <bool APIC, int AX, int OW, int OV>
+// Warps come in quads over blocks of 32 consecutive tile+halo cells (one cell
+// per lane): x faces / y faces / z faces / cell-centre density.  All four walk
+// the same particles at about the same time, so the later reads hit L1.  Each
+// lane walks its cell's particles once and accumulates, in registers, the
+// full 2x3x3 face stencil of its axis (faces of the cells at normal offset -1,
+// 0 and transverse offsets -1, 0, +1: the union of getFacesAround's 8-face
+// stencils over the cell) or the 3x3x3 stencil of getCellsAround -- the merged
+// contribution of all particles of the cell, at most 36 registers -- then adds
+// the entries inside the tile to the tile's shared accumulators (lanes hold
+// distinct cells, so a warp's adds never collide).  Measured on the 256^3 APIC
+// workload: 5.33 ms, against 5.69 ms for warp pairs (x + density / y + z, 72
+// accumulators, 168 registers, a 12x16x32 tile and one CTA per SM).
+template <bool APIC, int AX, int OW, int OV, int NA>
 __device__ __forceinline__ void p2g_face_axis(const float (&f)[3], const float (&wt)[3][3], float va,
-                                              const float* cm, float h, float zr, float (&acc)[NACC]) {
+                                              const float* cm, float h, float zr, float (&acc)[NA]) {
     constexpr int b = AX == 0 ? 1 : 0, c = AX == 2 ? 1 : 2;  // transverse axes, increasing
     const float wn[2] = {1.f - f[AX], f[AX]};
     float K = va, ka = 0.f, kb = 0.f, kc = 0.f;
@@ -105,10 +104,11 @@ __device__ __forceinline__ void p2g_face_axis(const float (&f)[3], const float (
         }
 }
 
-template <int AX, int OW, int OV>
-__device__ __forceinline__ void p2g_flush_axis(const float (&acc)[NACC], int cx, int cy, int cz, int x0, int y0,
+template <int AX, int OW, int OV, int NA, int TZ = PZ>
+__device__ __forceinline__ void p2g_flush_axis(const float (&acc)[NA], int cx, int cy, int cz, int x0, int y0,
                                                int z0, float* s_vw, float* s_w) {
     constexpr int b = AX == 0 ? 1 : 0, c = AX == 2 ? 1 : 2;
+    constexpr int NCELL = PX * PY * TZ;
 #pragma unroll
     for (int e = 0; e < 18; e++) {
         if (acc[OW + e] == 0.f) continue;
@@ -117,32 +117,32 @@ __device__ __forceinline__ void p2g_flush_axis(const float (&acc)[NACC], int cx,
         o[b] = (e / 3) % 3 - 1;
         o[c] = e % 3 - 1;
         const int lx = cx + o[0] - x0, ly = cy + o[1] - y0, lz = cz + o[2] - z0;
-        if (lx < 0 || ly < 0 || lz < 0 || lx >= PX || ly >= PY || lz >= PZ) continue;
-        const int li = (lx * PY + ly) * PZ + lz;
-        atomicAdd(&s_vw[AX * PCELLS + li], acc[OV + e]);
-        atomicAdd(&s_w[AX * PCELLS + li], acc[OW + e]);
+        if (lx < 0 || ly < 0 || lz < 0 || lx >= PX || ly >= PY || lz >= TZ) continue;
+        const int li = (lx * PY + ly) * TZ + lz;
+        atomicAdd(&s_vw[AX * NCELL + li], acc[OV + e]);
+        atomicAdd(&s_w[AX * NCELL + li], acc[OW + e]);
     }
 }
 
 template <bool APIC>
-__global__ void __launch_bounds__(P2G_THREADS_V2, 1) k_p2g(const P2GArgs a) {
+__global__ void __launch_bounds__(P2G_THREADS, 2) k_p2g(const P2GArgs a) {
     extern __shared__ float sm[];
-    float* s_vw = sm;              // [3][PCELLS] sum of w * contribution
-    float* s_w = sm + 3 * PCELLS;  // [3][PCELLS] sum of w
+    float* s_vw = sm;                // [3][PCELLS]
+    float* s_w = sm + 3 * PCELLS;   // [3][PCELLS]
     float* s_avg = sm + 6 * PCELLS;
     for (int k = threadIdx.x; k < 7 * PCELLS; k += blockDim.x) sm[k] = 0.f;
     const int bt = blockIdx.x;
     const int tz = bt % a.ntz, ty = (bt / a.ntz) % a.nty, tx = bt / (a.ntz * a.nty);
     const int x0 = tx * PX, y0 = ty * PY, z0 = tz * PZ;
     __syncthreads();
-    const float hinv = a.g.hinv, h = a.g.h, zr = a.g.two_d ? (float)(a.g.hzd * a.g.hinvd) : 1.f;
-    const float hinv3[3] = {hinv, hinv, a.g.hzinv};
+    const float h = a.g.h, zr = a.g.two_d ? (float)(a.g.hzd * a.g.hinvd) : 1.f;
+    const float hinv3[3] = {a.g.hinv, a.g.hinv, a.g.hzinv};
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int role = warp & 1;                  // 0: x faces + density, 1: y and z faces
-    const int pairs = P2G_THREADS_V2 / 64;      // warp pairs per CTA
+    const int role = warp & 3;
+    const int quads = P2G_THREADS / 128;
     constexpr int HC = QX * QY * QZ;
 
-    for (int blk = warp >> 1; blk * 32 < HC; blk += pairs) {
+    for (int blk = warp >> 2; blk * 32 < HC; blk += quads) {
         const int hc = blk * 32 + lane;
         if (hc >= HC) continue;
         const int hz = hc % QZ, hy = (hc / QZ) % QY, hx = hc / (QZ * QY);
@@ -152,10 +152,9 @@ __global__ void __launch_bounds__(P2G_THREADS_V2, 1) k_p2g(const P2GArgs a) {
         const int beg = a.cstart[cell], end = a.cstart[cell + 1];
         if (beg == end) continue;
         const int cc[3] = {cx, cy, cz};
-        float acc[NACC];
+        float acc[36];
 #pragma unroll
-        for (int e = 0; e < NACC; e++) acc[e] = 0.f;
-
+        for (int e = 0; e < 36; e++) acc[e] = 0.f;
         for (int k = beg; k < end; k++) {
             const uint32_t i = a.perm[k];
             float f[3];
@@ -164,46 +163,41 @@ __global__ void __launch_bounds__(P2G_THREADS_V2, 1) k_p2g(const P2GArgs a) {
             float wt[3][3];
 #pragma unroll
             for (int d = 0; d < 3; d++) tent3(f[d], wt[d]);
-            if (role == 0) {
-                float cm[3] = {0.f, 0.f, 0.f};
-                if (APIC) {
-#pragma unroll
-                    for (int q = 0; q < 3; q++) cm[q] = a.p.c[q][i];
-                }
-                p2g_face_axis<APIC, 0, 0, 18>(f, wt, a.p.v[0][i], cm, h, zr, acc);
+            if (role == 3) {
 #pragma unroll
                 for (int ox = 0; ox < 3; ox++)
 #pragma unroll
                     for (int oy = 0; oy < 3; oy++) {
                         const float wxy = wt[0][ox] * wt[1][oy];
 #pragma unroll
-                        for (int oz = 0; oz < 3; oz++) acc[36 + (ox * 3 + oy) * 3 + oz] += wxy * wt[2][oz];
+                        for (int oz = 0; oz < 3; oz++) acc[(ox * 3 + oy) * 3 + oz] += wxy * wt[2][oz];
                     }
             } else {
-                float cmy[3] = {0.f, 0.f, 0.f}, cmz[3] = {0.f, 0.f, 0.f};
+                float cm[3] = {0.f, 0.f, 0.f};
                 if (APIC) {
 #pragma unroll
-                    for (int q = 0; q < 3; q++) {
-                        cmy[q] = a.p.c[3 + q][i];
-                        cmz[q] = a.p.c[6 + q][i];
-                    }
+                    for (int q = 0; q < 3; q++) cm[q] = a.p.c[3 * role + q][i];
                 }
-                p2g_face_axis<APIC, 1, 0, 18>(f, wt, a.p.v[1][i], cmy, h, zr, acc);
-                p2g_face_axis<APIC, 2, 36, 54>(f, wt, a.p.v[2][i], cmz, h, zr, acc);
+                const float va = a.p.v[role][i];
+                if (role == 0) p2g_face_axis<APIC, 0, 0, 18>(f, wt, va, cm, h, zr, acc);
+                else if (role == 1) p2g_face_axis<APIC, 1, 0, 18>(f, wt, va, cm, h, zr, acc);
+                else p2g_face_axis<APIC, 2, 0, 18>(f, wt, va, cm, h, zr, acc);
             }
         }
-        if (role == 0) {
-            p2g_flush_axis<0, 0, 18>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
+        if (role == 3) {
 #pragma unroll
             for (int e = 0; e < 27; e++) {
-                if (acc[36 + e] == 0.f) continue;
+                if (acc[e] == 0.f) continue;
                 const int lx = cx + e / 9 - 1 - x0, ly = cy + (e / 3) % 3 - 1 - y0, lz = cz + e % 3 - 1 - z0;
                 if (lx < 0 || ly < 0 || lz < 0 || lx >= PX || ly >= PY || lz >= PZ) continue;
-                atomicAdd(&s_avg[(lx * PY + ly) * PZ + lz], acc[36 + e]);
+                atomicAdd(&s_avg[(lx * PY + ly) * PZ + lz], acc[e]);
             }
+        } else if (role == 0) {
+            p2g_flush_axis<0, 0, 18, 36, PZ>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
+        } else if (role == 1) {
+            p2g_flush_axis<1, 0, 18, 36, PZ>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
         } else {
-            p2g_flush_axis<1, 0, 18>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
-            p2g_flush_axis<2, 36, 54>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
+            p2g_flush_axis<2, 0, 18, 36, PZ>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
         }
     }
     __syncthreads();
@@ -445,14 +439,14 @@ void launch_p2g(fsim_ctx* ctx) {
     ctx->launches += 1;
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM_V2);
-        cudaFuncSetAttribute(k_p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM_V2);
+        cudaFuncSetAttribute(k_p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
+        cudaFuncSetAttribute(k_p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
         attr_set = true;
     }
     if (ctx->prm.transfer == FSIM_APIC)
-        k_p2g<true><<<nb, P2G_THREADS_V2, P2G_SMEM_V2, ctx->stream>>>(a);
+        k_p2g<true><<<nb, P2G_THREADS, P2G_SMEM, ctx->stream>>>(a);
     else
-        k_p2g<false><<<nb, P2G_THREADS_V2, P2G_SMEM_V2, ctx->stream>>>(a);
+        k_p2g<false><<<nb, P2G_THREADS, P2G_SMEM, ctx->stream>>>(a);
 }
 
 // P2G on caller-provided buffers (used by the allocation-free entry point in
@@ -471,12 +465,12 @@ void launch_p2g_raw(ParticleBuf p, const uint32_t* perm, const int* cstart, cons
     a.nty = ceil_div(g.ny, PY);
     a.ntz = ceil_div(g.nz, PZ);
     const int nb = a.ntx * a.nty * a.ntz;
-    cudaFuncSetAttribute(k_p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM_V2);
-    cudaFuncSetAttribute(k_p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM_V2);
+    cudaFuncSetAttribute(k_p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
+    cudaFuncSetAttribute(k_p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
     if (apic)
-        k_p2g<true><<<nb, P2G_THREADS_V2, P2G_SMEM_V2, stream>>>(a);
+        k_p2g<true><<<nb, P2G_THREADS, P2G_SMEM, stream>>>(a);
     else
-        k_p2g<false><<<nb, P2G_THREADS_V2, P2G_SMEM_V2, stream>>>(a);
+        k_p2g<false><<<nb, P2G_THREADS, P2G_SMEM, stream>>>(a);
 }
 
 // TMA descriptors of the six face arrays (v2 x/y/z, v x/y/z): 3D tensors
