@@ -155,11 +155,21 @@ __global__ void __launch_bounds__(P2G_THREADS, 2) k_p2g(const P2GArgs a) {
         float acc[36];
 #pragma unroll
         for (int e = 0; e < 36; e++) acc[e] = 0.f;
+        // software pipeline: the next particle's index and position are loaded
+        // while this one is accumulated (the kernel is latency-bound on these
+        // dependent loads; 5.31 -> 4.81 ms at 256^3)
+        uint32_t inext = a.perm[beg];
+        float pn[3] = {a.p.p[0][inext], a.p.p[1][inext], a.p.p[2][inext]};
         for (int k = beg; k < end; k++) {
-            const uint32_t i = a.perm[k];
+            const uint32_t i = inext;
             float f[3];
 #pragma unroll
-            for (int d = 0; d < 3; d++) f[d] = a.p.p[d][i] * hinv3[d] - (float)cc[d];
+            for (int d = 0; d < 3; d++) f[d] = pn[d] * hinv3[d] - (float)cc[d];
+            if (k + 1 < end) {
+                inext = a.perm[k + 1];
+#pragma unroll
+                for (int d = 0; d < 3; d++) pn[d] = a.p.p[d][inext];
+            }
             float wt[3][3];
 #pragma unroll
             for (int d = 0; d < 3; d++) tent3(f[d], wt[d]);
@@ -318,8 +328,30 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
     }
     __syncthreads();
     if (threadIdx.x >= 32 && threadIdx.x < 64) seg_pre[threadIdx.x + 1] += seg_pre[32];
+    __syncthreads();
+    const int total = seg_pre[TX * TY];
+    // sorted slot of the tile's j-th particle
+    auto slot_of = [&](int j) {
+        int lo = 0, hi = TX * TY - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (seg_pre[mid] <= j) lo = mid; else hi = mid - 1;
+        }
+        return seg_beg[lo] + (j - seg_pre[lo]);
+    };
+    // software pipeline: each thread's next particle (slot, index, position) is
+    // loaded one iteration ahead; the first one while the grid tile is in flight
+    int kn = 0;
+    uint32_t in = 0;
+    float pn[3] = {0.f, 0.f, 0.f};
+    if ((int)threadIdx.x < total) {
+        kn = slot_of(threadIdx.x);
+        in = a.perm[kn];
+        pn[0] = a.src.p[0][in]; pn[1] = a.src.p[1][in]; pn[2] = a.src.p[2][in];
+    }
     // wait for the staged grid (bounded: about 2^31 cycles, then report and leave;
-    // the leave decision is made for the whole CTA at once)
+    // the leave decision is made for the whole CTA at once, after a second bounded
+    // wait for the copies still in flight)
     {
         const long long t0 = clock64();
         bool ok = false;
@@ -327,21 +359,26 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
             if (clock64() - t0 > (1ll << 31)) break;
         }
         if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) atomicOr(a.err, FSIM_DERR_TMA_TIMEOUT);
+            if (threadIdx.x == 0) {
+                atomicOr(a.err, FSIM_DERR_TMA_TIMEOUT);
+                const long long t1 = clock64();
+                while (!mbar_try_wait(&mbar, 0) && clock64() - t1 < (1ll << 31)) {
+                }
+            }
+            __syncthreads();
             return;
         }
     }
-    const int total = seg_pre[TX * TY];
     const float hinv = a.g.hinv, hzinv = a.g.hzinv;
     for (int j = threadIdx.x; j < total; j += blockDim.x) {
-        int lo = 0, hi = TX * TY - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (seg_pre[mid] <= j) lo = mid; else hi = mid - 1;
+        const int k = kn;
+        const uint32_t i = in;
+        const float px = pn[0], py = pn[1], pz = pn[2];
+        if (j + (int)blockDim.x < total) {
+            kn = slot_of(j + blockDim.x);
+            in = a.perm[kn];
+            pn[0] = a.src.p[0][in]; pn[1] = a.src.p[1][in]; pn[2] = a.src.p[2][in];
         }
-        const int k = seg_beg[lo] + (j - seg_pre[lo]);
-        const uint32_t i = a.perm[k];
-        const float px = a.src.p[0][i], py = a.src.p[1][i], pz = a.src.p[2][i];
         const float g[3] = {px * hinv, py * hinv, pz * hzinv};
         float vnew[3];
         float cnew[9];
