@@ -522,7 +522,7 @@ constexpr int MIXED_REFINE_DIGITS = 3;
 constexpr int MG_NU_DEFAULT = 2;           // level 0
 constexpr int MG_NU_COARSE_DEFAULT = 6;    // level 1 and other separately launched levels
 constexpr int MG_NU_CLUSTER_DEFAULT = 6;   // levels run by the cluster kernel
-constexpr int MG_BOTTOM_SWEEPS = 12;
+constexpr int MG_BOTTOM_SWEEPS = 4;  // on the <= 4^3 bottom level; 12 gave the same iterations, 12 us/it slower
 constexpr int MG_BOTTOM_MAX = 4096;
 
 struct MGLev {
