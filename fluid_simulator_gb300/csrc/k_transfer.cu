@@ -72,8 +72,9 @@ __device__ __forceinline__ void tent3(float f, float (&w)[3]) {
 // contribution of all particles of the cell, at most 36 registers -- then adds
 // the entries inside the tile to the tile's shared accumulators (lanes hold
 // distinct cells, so a warp's adds never collide).  Measured on the 256^3 APIC
-// workload: 5.33 ms, against 5.69 ms for warp pairs (x + density / y + z, 72
-// accumulators, 168 registers, a 12x16x32 tile and one CTA per SM).
+// workload (before the one-ahead loads below): 5.33 ms, against 5.69 ms for warp
+// pairs (x + density / y + z, 72 accumulators, 168 registers, a 12x16x32 tile
+// and one CTA per SM).
 template <bool APIC, int AX, int OW, int OV, int NA>
 __device__ __forceinline__ void p2g_face_axis(const float (&f)[3], const float (&wt)[3][3], float va,
                                               const float* cm, float h, float zr, float (&acc)[NA]) {
