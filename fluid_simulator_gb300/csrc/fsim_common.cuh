@@ -8,6 +8,25 @@
 
 #include "../../include/fsim.h"
 
+#include <mutex>
+#include <set>
+#include <utility>
+
+// Raises a kernel's dynamic shared-memory limit on the current device, once per
+// (kernel, device) and thread-safe; later calls only look the pair up.
+inline cudaError_t set_smem_limit(const void* kern, int bytes) {
+    static std::mutex mu;
+    static std::set<std::pair<const void*, int>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count({kern, dev})) return cudaSuccess;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) done.insert({kern, dev});
+    return e;
+}
+
 #define FSIM_MAX_OBS 32
 #define FSIM_DEAD_KEY 0xFFFFFFFFu
 

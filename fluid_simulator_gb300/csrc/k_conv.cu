@@ -528,22 +528,10 @@ int launch_conv_mma(const ConvLaunch& L, cudaStream_t s) {
     const long long grid = (long long)a.tiles_w * a.tiles_h * a.tiles_d * L.n * a.ntiles;
     if (grid <= 0) return FSIM_OK;
     if (taps == 27) {
-        static bool attr = false;
-        if (!attr) {
-            if (cudaFuncSetAttribute(k_conv_mma<27>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_LIMIT) !=
-                cudaSuccess)
-                return FSIM_E_CUDA;
-            attr = true;
-        }
+        if (set_smem_limit((const void*)k_conv_mma<27>, SMEM_LIMIT) != cudaSuccess) return FSIM_E_CUDA;
         k_conv_mma<27><<<(unsigned)grid, CONV_THREADS, smem, s>>>(a, *L.mx, *L.mw);
     } else {
-        static bool attr = false;
-        if (!attr) {
-            if (cudaFuncSetAttribute(k_conv_mma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_LIMIT) !=
-                cudaSuccess)
-                return FSIM_E_CUDA;
-            attr = true;
-        }
+        if (set_smem_limit((const void*)k_conv_mma<1>, SMEM_LIMIT) != cudaSuccess) return FSIM_E_CUDA;
         k_conv_mma<1><<<(unsigned)grid, CONV_THREADS, smem, s>>>(a, *L.mx, *L.mw);
     }
     return cudaGetLastError() == cudaSuccess ? FSIM_OK : FSIM_E_CUDA;
@@ -576,13 +564,7 @@ int launch_conv_wgrad(const WgradLaunch& L, cudaStream_t s) {
     a.err = L.err;
     const int stage = 2 * (mt * 128 * 16) + 2 * L.cout * 16;
     const int smem = 2 * stage + 128;
-    static bool attr = false;
-    if (!attr) {
-        if (cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_LIMIT) !=
-            cudaSuccess)
-            return FSIM_E_CUDA;
-        attr = true;
-    }
+    if (set_smem_limit((const void*)k_conv_wgrad, SMEM_LIMIT) != cudaSuccess) return FSIM_E_CUDA;
     k_conv_wgrad<<<(unsigned)(a.groups * a.ksplit), CONV_THREADS, smem, s>>>(a);
     return cudaGetLastError() == cudaSuccess ? FSIM_OK : FSIM_E_CUDA;
 }

@@ -475,12 +475,8 @@ void launch_p2g(fsim_ctx* ctx) {
     a.ntz = ceil_div(g.nz, PZ);
     const int nb = a.ntx * a.nty * a.ntz;
     ctx->launches += 1;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
-        cudaFuncSetAttribute(k_p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
-        attr_set = true;
-    }
+    set_smem_limit((const void*)k_p2g<false>, P2G_SMEM);
+    set_smem_limit((const void*)k_p2g<true>, P2G_SMEM);
     if (ctx->prm.transfer == FSIM_APIC)
         k_p2g<true><<<nb, P2G_THREADS, P2G_SMEM, ctx->stream>>>(a);
     else
@@ -503,8 +499,8 @@ void launch_p2g_raw(ParticleBuf p, const uint32_t* perm, const int* cstart, cons
     a.nty = ceil_div(g.ny, PY);
     a.ntz = ceil_div(g.nz, PZ);
     const int nb = a.ntx * a.nty * a.ntz;
-    cudaFuncSetAttribute(k_p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
-    cudaFuncSetAttribute(k_p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, P2G_SMEM);
+    set_smem_limit((const void*)k_p2g<false>, P2G_SMEM);
+    set_smem_limit((const void*)k_p2g<true>, P2G_SMEM);
     if (apic)
         k_p2g<true><<<nb, P2G_THREADS, P2G_SMEM, stream>>>(a);
     else
@@ -561,13 +557,9 @@ int launch_g2p(fsim_ctx* ctx) {
     const int mode = ctx->prm.transfer;
     ctx->launches += 1;
     const size_t smem = (size_t)((mode == FSIM_FLIP) ? 6 : 3) * BOXN * sizeof(float);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_g2p<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * BOXN * 4);
-        cudaFuncSetAttribute(k_g2p<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 6 * BOXN * 4);
-        cudaFuncSetAttribute(k_g2p<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * BOXN * 4);
-        attr_set = true;
-    }
+    set_smem_limit((const void*)k_g2p<0>, 3 * BOXN * 4);
+    set_smem_limit((const void*)k_g2p<1>, 6 * BOXN * 4);
+    set_smem_limit((const void*)k_g2p<2>, 3 * BOXN * 4);
     const CUtensorMap* m = ctx->tmap;
     if (mode == FSIM_PIC)
         k_g2p<0><<<nb, G2P_THREADS, smem, ctx->stream>>>(a, m[0], m[1], m[2], m[3], m[4], m[5]);

@@ -4,9 +4,11 @@
 // obstacles, call simulate(dt) K times, read the particles back through
 // getParticleAt.  Input / output: raw float32 arrays (pos n x 3).
 //
-//   facade_demo <resolution> <steps> <dt> <transfer 0|1|2> <in_pos.bin> <out.bin> [basic]
+//   facade_demo <resolution> <steps> <dt> <transfer 0|1|2> <in_pos.bin> <out.bin> [basic|2d]
 //
-// With "basic", the grid is a BasicMacGrid (the SOR solver).
+// With "basic", the grid is a BasicMacGrid (the SOR solver); with "2d" the
+// grid and the particles are built in 2D mode (dims (1, 1, 0.3), particles on
+// z = 0.15), as SimulationManager does for twoD (simulationManager.cpp:17,27).
 //
 // out.bin: int64 n, then pos (n x 3), v (n x 3), c (n x 9) as float32, then
 // int32 PCG iterations of the last step.
@@ -23,10 +25,13 @@ using namespace genericfsim;
 
 int main(int argc, char** argv) {
     if (argc != 7 && argc != 8) {
-        std::cerr << "usage: facade_demo res steps dt transfer in_pos.bin out.bin [basic]\n";
+        std::cerr << "usage: facade_demo res steps dt transfer in_pos.bin out.bin [basic|2d]\n";
         return 2;
     }
     const bool basic = argc == 8 && std::string(argv[7]) == "basic";
+    const bool two_d = argc == 8 && std::string(argv[7]) == "2d";
+    const glm::dvec3 dims = two_d ? glm::dvec3(1, 1, 0.3) : glm::dvec3(1, 1, 1);
+    const double zc = two_d ? 0.15 : 0.5;
     const double res = std::atof(argv[1]);
     const int steps = std::atoi(argv[2]);
     const double dt = std::atof(argv[3]);
@@ -39,14 +44,15 @@ int main(int argc, char** argv) {
     const size_t n = pos.size() / 3;
     try {
         std::shared_ptr<macgrid::MacGrid> grid;
-        if (basic) grid = std::make_shared<macgrid::BasicMacGrid>(glm::dvec3(1, 1, 1), res, false);
-        else grid = std::make_shared<macgrid::BridsonSolverGrid>(glm::dvec3(1, 1, 1), (float)res, false, 1.0);
+        if (basic) grid = std::make_shared<macgrid::BasicMacGrid>(dims, res, two_d);
+        else grid = std::make_shared<macgrid::BridsonSolverGrid>(dims, (float)res, two_d, 1.0);
         grid->isTopOfContainerSolid = true;
         grid->pressureEnabled = false;
         grid->incompressibilityMaxIterationCount = 200;
         grid->residualTolerance = 1e-6;
         const double h = 1.0 / res;
-        auto parts = std::make_shared<particles::HashedParticles>(0, h / 4, grid->dimensions, grid->cellD, false, 0.0);
+        auto parts = std::make_shared<particles::HashedParticles>(0, h / 4, grid->dimensions, grid->cellD, two_d,
+                                                                  dims.z / 2);
         std::vector<particles::Particle> ps(n);
         for (size_t i = 0; i < n; i++) {
             ps[i].pos = glm::dvec3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
@@ -60,9 +66,9 @@ int main(int argc, char** argv) {
         cfg.gravity = -9.81f;
         cfg.pushApartEnabled = false;
         simulator::Simulator sim(cfg, parts, grid);
-        sim.obstacles.push_back(std::make_unique<obstacle::SphericalObstacle>(0.15, glm::dvec3(0.6, 0.3, 0.5)));
+        sim.obstacles.push_back(std::make_unique<obstacle::SphericalObstacle>(0.15, glm::dvec3(0.6, 0.3, zc)));
         for (int s = 0; s < steps; s++) {
-            sim.obstacles[0]->setNewPos(glm::dvec3(0.6 + 0.01 * s, 0.3, 0.5));
+            sim.obstacles[0]->setNewPos(glm::dvec3(0.6 + 0.01 * s, 0.3, zc));
             sim.obstacles[0]->calculateSpeed(dt);
             sim.simulate(dt);
         }
@@ -79,7 +85,7 @@ int main(int argc, char** argv) {
             }
         }
         // a cell read through the grid mirror, as SimulationManager::getCellAt does
-        const macgrid::MacGridCell& cell = grid->getCellAt(glm::dvec3(0.3, 0.1, 0.5));
+        const macgrid::MacGridCell& cell = grid->getCellAt(glm::dvec3(0.3, 0.1, zc));
         std::ofstream out(argv[6], std::ios::binary);
         const int64_t mm = m;
         out.write(reinterpret_cast<const char*>(&mm), 8);

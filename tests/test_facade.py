@@ -27,23 +27,26 @@ def test_facade_compiles():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("transfer,basic", [(1, False), (2, False), (1, True)])
-def test_facade_matches_c_abi(gpu, tmp_path, transfer, basic):
+@pytest.mark.parametrize("transfer,mode", [(1, ""), (2, ""), (1, "basic"), (2, "2d")])
+def test_facade_matches_c_abi(gpu, tmp_path, transfer, mode):
     from fluid_simulator_gb300 import native as N
-    from fluid_simulator_gb300.scenes import GridSpec, dam_break
+    from fluid_simulator_gb300.scenes import GridSpec, dam_break, dam_break_2d
 
     exe = tmp_path / "facade_demo"
     r = subprocess.run(["g++", "-std=c++17", "-O2", f"-I{GLM}", f"-I{INC}", DEMO, "-o", str(exe), f"-L{LIBDIR}",
                         "-lfsim", f"-Wl,-rpath,{LIBDIR}"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     res, steps, dt = 32, 6, 1.0 / 120.0
-    grid = GridSpec(res)
-    pos = dam_break(grid, seed=3)
+    basic, two_d = mode == "basic", mode == "2d"
+    dims = (1.0, 1.0, 0.3) if two_d else (1.0, 1.0, 1.0)
+    zc = dims[2] / 2 if two_d else 0.5
+    grid = GridSpec(res, dims, two_d)
+    pos = dam_break_2d(grid, seed=3) if two_d else dam_break(grid, seed=3)
     inp = tmp_path / "pos.bin"
     out = tmp_path / "out.bin"
     pos.astype(np.float32).tofile(inp)
     r = subprocess.run([str(exe), str(res), str(steps), repr(dt), str(transfer), str(inp), str(out)] +
-                       (["basic"] if basic else []), capture_output=True, text=True, timeout=300)
+                       ([mode] if mode else []), capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr + r.stdout
     raw = out.read_bytes()
     n = int(np.frombuffer(raw[:8], np.int64)[0])
@@ -56,13 +59,13 @@ def test_facade_matches_c_abi(gpu, tmp_path, transfer, basic):
                          tol=1e-6, tol_mode=N.TOL_ABS_MAX, precision=N.PREC_MIXED, warm_start=N.WARM_ZERO,
                          top_solid=True, particle_r=h / 4, pressure_enabled=False, timing=True,
                          precond=N.PRECOND_MG, grid_solver=N.SOLVER_SOR if basic else N.SOLVER_PCG)
-    sim = N.Simulation(res, p)
+    sim = N.Simulation(res, p, dims=dims, two_d=two_d)
     sim.set_particles(pos)
     st = None
     for s in range(steps):
         x = 0.6 + 0.01 * s
         xp = 0.6 + 0.01 * (s - 1) if s > 0 else 0.6
-        sim.set_obstacles([N.obstacle(N.OBS_SPHERE, (x, 0.3, 0.5), r=0.15, prev_pos=(xp, 0.3, 0.5),
+        sim.set_obstacles([N.obstacle(N.OBS_SPHERE, (x, 0.3, zc), r=0.15, prev_pos=(xp, 0.3, zc),
                                       speed=((x - xp) / dt, 0.0, 0.0))])
         st = sim.step(dt)
     gp, gv, gc = sim.particles()
