@@ -396,6 +396,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_spmv(const PcgArgs a, Vecs<T> v
     T* sn = sc ? v.s[0] : v.s[1];
     Acc<T> sq;
     const T betaT = (T)beta;
+    const bool beta0 = beta == 0.0;
     const int nact = *a.nactive;
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int x, y, z;
@@ -403,13 +404,15 @@ __global__ void __launch_bounds__(PCG_THREADS) k_spmv(const PcgArgs a, Vecs<T> v
         if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, z, c)) continue;
         const uint16_t cc = a.code[c];
         if (!(cc & CODE_FLUID)) continue;
-        const T snc = v.z[c] + betaT * so[c];
+        // beta = 0 (first iteration, after a restart): s = z exactly, without
+        // reading s_old (which may hold a previous solve's non-finite values)
+        const T snc = beta0 ? v.z[c] : v.z[c] + betaT * so[c];
         T qv = (T)code_ns(cc) * snc;
 #pragma unroll
         for (int k = 0; k < 6; k++)
             if ((cc >> k) & 1) {
                 const long long j = c + nb_off(a.B, k);
-                qv -= v.z[j] + betaT * so[j];
+                qv -= beta0 ? v.z[j] : v.z[j] + betaT * so[j];
             }
         sn[c] = snc;
         v.q[c] = qv;
@@ -863,20 +866,23 @@ __global__ void __launch_bounds__(PCG_THREADS) k_spmv_q(const PcgArgs a, Vecs<fl
         uint16_t cc[4];
         codes4(a.code, c0, cc);
         if (!any_fluid(cc)) return;
-        Q7 zq, sq7;
+        Q7 zq;
         load_q7(zq, v.z, c0, L, x, y, z0);
-        load_q7(sq7, so, c0, L, x, y, z0);
-        Q7 n;  // s_new around the quad
+        Q7 n = zq;  // s_new around the quad; beta = 0: s = z, s_old is not read
+        if (beta != 0.f) {
+            Q7 sq7;
+            load_q7(sq7, so, c0, L, x, y, z0);
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            n.c[i] = zq.c[i] + beta * sq7.c[i];
-            n.xp[i] = zq.xp[i] + beta * sq7.xp[i];
-            n.xm[i] = zq.xm[i] + beta * sq7.xm[i];
-            n.yp[i] = zq.yp[i] + beta * sq7.yp[i];
-            n.ym[i] = zq.ym[i] + beta * sq7.ym[i];
+            for (int i = 0; i < 4; i++) {
+                n.c[i] = zq.c[i] + beta * sq7.c[i];
+                n.xp[i] = zq.xp[i] + beta * sq7.xp[i];
+                n.xm[i] = zq.xm[i] + beta * sq7.xm[i];
+                n.yp[i] = zq.yp[i] + beta * sq7.yp[i];
+                n.ym[i] = zq.ym[i] + beta * sq7.ym[i];
+            }
+            n.zm = zq.zm + beta * sq7.zm;
+            n.zp = zq.zp + beta * sq7.zp;
         }
-        n.zm = zq.zm + beta * sq7.zm;
-        n.zp = zq.zp + beta * sq7.zp;
         float qv[4], snc[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
