@@ -507,9 +507,31 @@ def warm_start_study(sim, dt, t, h, N, args):
         sim.stage(N.STAGE_EXTRAPOLATE, dt)
         sim.stage(N.STAGE_G2P, dt)
         t += dt
+
+    # whole steps (fsim_step; the library's CUDA events from the first to the last
+    # stage) with each start, one after the other on the running scene
+    def steps_per_s(mode, backoff, n=5):
+        nonlocal t
+        keep = (sim.params.warm_start, sim.params.learned_backoff)
+        sim.params.warm_start, sim.params.learned_backoff = mode, backoff
+        sim.set_params(sim.params)
+        ms = []
+        for k in range(n + 1):
+            sim.set_obstacles(obstacles_at(t, dt, h, N))
+            st = sim.step(dt)
+            t += dt
+            if k > 0:
+                ms.append(st.ms_total)
+        sim.params.warm_start, sim.params.learned_backoff = keep
+        sim.set_params(sim.params)
+        return round(1000.0 / statistics.mean(ms), 3)
+
+    whole = {"zero": steps_per_s(N.WARM_ZERO, 0), "previous": steps_per_s(N.WARM_PREVIOUS, 0),
+             "learned_backoff": steps_per_s(N.WARM_LEARNED, 1)}
     sim.set_net(None)
     net.close()
-    out = {"tol": "1e-6 relative L2", "problems": args.ws_steps, "training": info}
+    out = {"tol": "1e-6 relative L2", "problems": args.ws_steps, "training": info,
+           "steps_per_s": whole}
     for name, _ in modes:
         r = rec[name]
         out[name] = {"ms": round(statistics.mean(x[0] for x in r), 3),
