@@ -402,9 +402,10 @@ def render_study(sim, N, h, peak):
     n = sim.n
     covered = int((r.read(N.IMG_RAW_DEPTH) < 1.0).sum())
     r.close()
-    # algorithmic bytes: three particle passes over the 20-byte records (surface
-    # splat, spray splat, thickness splat) + the image passes (~120 B per pixel)
-    alg = 3 * 20 * n + 120 * W * H
+    # algorithmic bytes: two particle passes over the 20-byte records (surface
+    # splat and spray splat, each also adding thickness) + the image passes
+    # (~120 B per pixel)
+    alg = 2 * 20 * n + 120 * W * H
     k = statistics.median(kernel_ms)
     return {"image": [W, H], "particles": n, "covered_pixels": covered, "ms_per_frame_kernels": round(k, 3),
             "ms_per_frame_wall": round(wall_ms, 3), "launches_per_frame": launches,

@@ -13,7 +13,9 @@
 //   3. spray particles (density below the threshold) splatted onto the
 //      smoothed depth;
 //   4. additive thickness splat (particle_sprites_thickness.fs) depth-tested
-//      against the scene, then its separable blur (gaussian_thickness.fs);
+//      against the scene -- computed by passes 1 and 3 from the same fragments,
+//      which cover every particle once -- then its separable blur
+//      (gaussian_thickness.fs);
 //   5. normals from the smoothed depth (normal_depth.fs);
 //   6. Blinn-Phong shading with Perlin surface noise and thickness
 //      transparency, blended over the background (shadedDepth.fs).
@@ -178,9 +180,14 @@ __device__ __forceinline__ float window_depth(const Cam& cam, const float* p, bo
     return z * 0.5f + 0.5f;
 }
 
-// which: 0 all particles, 1 surface (density >= threshold), 2 spray (below)
+// which: 0 all particles, 1 surface (density >= threshold), 2 spray (below).
+// With `thick` set, the same fragments also add their thickness
+// (particle_sprites_thickness.fs: sqrt(1 - r2) * r, GL_ONE + GL_ONE blending),
+// depth-tested GL_LESS against the scene depth at the billboard plane and not
+// against the fluid depth, so one pass per particle serves both splats (the
+// surface and the spray passes together cover every particle once).
 __global__ void k_splat_depth(const fsim_particle_gfx* parts, long long n, int which, float thr, Cam cam, float r,
-                              int W, int H, unsigned* depth_bits) {
+                              int W, int H, unsigned* depth_bits, const float* scene, float* thick) {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const fsim_particle_gfx pg = parts[k];
@@ -193,12 +200,14 @@ __global__ void k_splat_depth(const fsim_particle_gfx* parts, long long n, int w
             float px, py, P[3];
             if (!sprite_hit(cam, s, r, W, H, i, j, px, py, P)) continue;
             bool inside;
-            window_depth(cam, P, inside);
+            const float zq = window_depth(cam, P, inside);
             if (!inside) continue;
             // particle_sprites_depth.fs
             const float nx = px * 2.f, ny = -py * 2.f;  // texCoord * 2 - 1
             const float r2 = nx * nx + ny * ny;
             if (r2 > 1.f) continue;
+            const long long pix = (long long)j * W + i;
+            if (thick && zq < (scene ? scene[pix] : 1.f)) atomicAdd(&thick[pix], sqrtf(1.f - r2) * r);
             const float nz = -sqrtf(1.f - r2);
             float nrm[3];
 #pragma unroll
@@ -210,29 +219,7 @@ __global__ void k_splat_depth(const fsim_particle_gfx* parts, long long n, int w
             bool in2;
             float z = window_depth(cam, pp, in2);
             z = fminf(fmaxf(z, 0.f), 1.f);  // gl_FragDepth is clamped to the depth range
-            atomicMin(&depth_bits[(long long)j * W + i], __float_as_uint(z));  // z >= 0: bits order as floats
-        }
-}
-
-__global__ void k_splat_thickness(const fsim_particle_gfx* parts, long long n, Cam cam, float r, int W, int H,
-                                  const float* scene, float* thick) {
-    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    Sprite s;
-    if (!make_sprite(cam, parts[k].pos, r, W, H, s)) return;
-    for (int j = s.y0; j <= s.y1; j++)
-        for (int i = s.x0; i <= s.x1; i++) {
-            float px, py, P[3];
-            if (!sprite_hit(cam, s, r, W, H, i, j, px, py, P)) continue;
-            bool inside;
-            const float z = window_depth(cam, P, inside);
-            if (!inside) continue;
-            const float sd = scene ? scene[(long long)j * W + i] : 1.f;
-            if (!(z < sd)) continue;  // GL_LESS against the scene, no depth write
-            const float nx = px * 2.f, ny = -py * 2.f;
-            const float r2 = nx * nx + ny * ny;
-            if (r2 > 1.f) continue;
-            atomicAdd(&thick[(long long)j * W + i], sqrtf(1.f - r2) * r);  // GL_ONE, GL_ONE
+            atomicMin(&depth_bits[pix], __float_as_uint(z));  // z >= 0: bits order as floats
         }
 }
 
@@ -732,12 +719,15 @@ int fsim_render_frame(fsim_renderer* r, const fsim_particle_gfx* particles, int6
     const float rad = prm->particle_radius;
     int L = 0;
     cudaEventRecord(r->ev0, s);
-    // 1. surface sprites into the cleared depth buffer
+    // 1. surface sprites into the cleared depth buffer, with their thickness
+    //    (the thickness of all particles accumulates over passes 1 and 3)
+    float* thick = prm->transparency_enabled ? r->thick : nullptr;
     k_fill<<<nblk(np), 256, 0, s>>>(r->raw, np, 1.f);
-    L++;
+    k_fill<<<nblk(np), 256, 0, s>>>(r->thick, np, 0.f);
+    L += 2;
     if (n > 0) {
         k_splat_depth<<<nblk(n), 256, 0, s>>>(dp, n, prm->spray_enabled ? 1 : 0, prm->spray_density_threshold, k,
-                                              rad, W, H, reinterpret_cast<unsigned*>(r->raw));
+                                              rad, W, H, reinterpret_cast<unsigned*>(r->raw), scene_depth, thick);
         L++;
     }
     // 2. smoothing, x into tmp then y into depth
@@ -750,17 +740,11 @@ int fsim_render_frame(fsim_renderer* r, const fsim_particle_gfx* particles, int6
     // 3. spray on top of the smoothed surface
     if (prm->spray_enabled && n > 0) {
         k_splat_depth<<<nblk(n), 256, 0, s>>>(dp, n, 2, prm->spray_density_threshold, k, rad, W, H,
-                                              reinterpret_cast<unsigned*>(r->depth));
+                                              reinterpret_cast<unsigned*>(r->depth), scene_depth, thick);
         L++;
     }
-    // 4. thickness of all particles, blurred x then y
-    k_fill<<<nblk(np), 256, 0, s>>>(r->thick, np, 0.f);
-    L++;
+    // 4. thickness blurred x then y
     if (prm->transparency_enabled) {
-        if (n > 0) {
-            k_splat_thickness<<<nblk(n), 256, 0, s>>>(dp, n, k, rad, W, H, scene_depth, r->thick);
-            L++;
-        }
         k_blur<<<nblk(np), 256, 0, s>>>(2, 0, r->thick, r->depth, r->ttmp, W, H, k, prm->transparency_blur_size,
                                        0.f, 0.f);
         k_blur<<<nblk(np), 256, 0, s>>>(2, 1, r->ttmp, r->depth, r->thick, W, H, k, prm->transparency_blur_size,
