@@ -245,6 +245,7 @@ struct PcgArgs {
     unsigned* counter;
     double tol_abs, tol_rel;  // tolerance in A' units (abs) / relative
     double skip_bb;           // early-out threshold on b'.b' (reference: sum b^2 < 1e-7)
+    int phi_zero;             // the solve starts from phi = 0 (its first residual is b)
 };
 
 template <typename T>
@@ -271,10 +272,13 @@ __global__ void __launch_bounds__(PCG_THREADS) k_residual(const PcgArgs a, Vecs<
         const uint16_t cc = a.code[c];
         if (!(cc & CODE_FLUID)) continue;
         const double* phi = a.phi;
-        double ap = (double)code_ns(cc) * phi[c];
+        double ap = 0.0;
+        if (!(first && a.phi_zero)) {  // from a zero start the first residual is b itself
+            ap = (double)code_ns(cc) * phi[c];
 #pragma unroll
-        for (int k = 0; k < 6; k++)
-            if ((cc >> k) & 1) ap -= phi[c + nb_off(a.B, k)];
+            for (int k = 0; k < 6; k++)
+                if ((cc >> k) & 1) ap -= phi[c + nb_off(a.B, k)];
+        }
         const double bc = a.b[c];
         const double rv = bc - ap;
         r[c] = (T)rv;
@@ -1854,6 +1858,7 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     A.tol_abs = tol / scale;
     A.tol_rel = tol;
     A.skip_bb = rhs_override ? -1.0 : 1e-7 / (scale * scale);
+    A.phi_zero = (warm == FSIM_WARM_ZERO && !judged) ? 1 : 0;
 
     int rc;
     if (judged) {
