@@ -696,8 +696,10 @@ int fsim_stage(fsim_ctx* ctx, int stage, double dt, fsim_step_stats* stats) {
                 CHECK_LAUNCH(ctx);
                 break;
             }
+            const long long l0 = ctx->launches;
             rc = solve_pressure(ctx, dt, P.precision, P.tol_mode, P.residual_tol, P.max_iters, P.warm_start, sp,
                                 nullptr, 1);
+            sp->kernel_launches = (int)(ctx->launches - l0);
             break;
         }
         case FSIM_STAGE_EXTRAPOLATE: launch_extrapolate(ctx); CHECK_LAUNCH(ctx); break;
