@@ -74,6 +74,9 @@ constexpr float SAFE = 0.25f;
 
 // code bits
 constexpr uint16_t CODE_FLUID = 0x8000;
+// shared-memory copies of the codes (coarsest multigrid levels) also carry the
+// cell's colour, (x + y + z) & 1, so that a half sweep needs no coordinates
+constexpr uint16_t SCODE_ODD = 0x4000;
 __device__ __forceinline__ int code_ns(uint16_t c) { return (c >> 8) & 7; }
 __device__ __forceinline__ int code_nf(uint16_t c) { return __popc(c & 0x3F); }
 
@@ -1004,10 +1007,12 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update_q(const PcgArgs a, Vecs<
 __device__ void mg_bottom_block(const MGLev& L, float* sx, float* sf, uint16_t* sc) {
     const int n = L.nx * L.ny * L.nz;  // dense in shared memory, padded in global
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const long long gi = (long long)(i / L.nz) * L.pz + (i % L.nz);
+        const int z = i % L.nz, t = i / L.nz;
+        const long long gi = (long long)t * L.pz + z;
+        const int odd = (t / L.ny + t % L.ny + z) & 1;
         sx[i] = 0.f;
         sf[i] = L.f[gi];
-        sc[i] = L.code[gi];
+        sc[i] = L.code[gi] | (odd ? SCODE_ODD : 0);
     }
     __syncthreads();
     const int sxs = L.ny * L.nz, sys = L.nz;
@@ -1015,11 +1020,10 @@ __device__ void mg_bottom_block(const MGLev& L, float* sx, float* sf, uint16_t* 
         // forward half: red then black; backward half: black then red
         for (int h = 0; h < 2; h++) {
             const int color = (pass < MG_BOTTOM_SWEEPS) ? h : 1 - h;
+            const uint16_t want = CODE_FLUID | (color ? SCODE_ODD : 0);
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                const int z = i % L.nz, y = (i / L.nz) % L.ny, x = i / sxs;
-                if (((x + y + z) & 1) != color) continue;
                 const uint16_t cc = sc[i];
-                if (!(cc & CODE_FLUID)) continue;
+                if ((cc & (CODE_FLUID | SCODE_ODD)) != want) continue;
                 float sum = sf[i];
                 if (cc & 1) sum += sx[i + sxs];
                 if (cc & 2) sum += sx[i - sxs];
@@ -1079,17 +1083,17 @@ struct SLev {
 
 __device__ __forceinline__ int sidx(const SLev& L, int x, int y, int z) { return (x * L.ny + y) * L.nz + z; }
 
-__device__ void s_smooth(const SLev& L, int color) {
+__device__ void s_smooth(const SLev L, int color) {
+    const int sx = L.ny * L.nz, sy = L.nz;
+    const uint16_t want = CODE_FLUID | (color ? SCODE_ODD : 0);
     for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
-        const int z = i % L.nz, y = (i / L.nz) % L.ny, x = i / (L.nz * L.ny);
-        if (((x + y + z) & 1) != color) continue;
         const uint16_t cc = L.code[i];
-        if (!(cc & CODE_FLUID)) continue;
+        if ((cc & (CODE_FLUID | SCODE_ODD)) != want) continue;
         float s = 0.f;
-        if (cc & 1) s += L.x[i + L.ny * L.nz];
-        if (cc & 2) s += L.x[i - L.ny * L.nz];
-        if (cc & 4) s += L.x[i + L.nz];
-        if (cc & 8) s += L.x[i - L.nz];
+        if (cc & 1) s += L.x[i + sx];
+        if (cc & 2) s += L.x[i - sx];
+        if (cc & 4) s += L.x[i + sy];
+        if (cc & 8) s += L.x[i - sy];
         if (cc & 16) s += L.x[i + 1];
         if (cc & 32) s += L.x[i - 1];
         L.x[i] = (L.f[i] + s) * c_rcp[code_ns(cc)];
@@ -1097,7 +1101,7 @@ __device__ void s_smooth(const SLev& L, int color) {
     __syncthreads();
 }
 
-__device__ void s_residual(const SLev& L) {
+__device__ void s_residual(const SLev L) {
     for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
         const uint16_t cc = L.code[i];
         float rv = 0.f;
@@ -1119,7 +1123,7 @@ __device__ void s_residual(const SLev& L) {
 __device__ __forceinline__ float fw_weight(int d) { return (d == 0 || d == 1) ? 0.75f : 0.25f; }
 
 // coarse f = 0.5 * sum_fine P r (fine fluid only), coarse x = 0
-__device__ void s_restrict(const SLev& F, const SLev& C) {
+__device__ void s_restrict(const SLev F, const SLev C) {
     for (int i = threadIdx.x; i < C.n; i += blockDim.x) {
         const int cz = i % C.nz, cy = (i / C.nz) % C.ny, cx = i / (C.nz * C.ny);
         C.x[i] = 0.f;
@@ -1149,7 +1153,7 @@ __device__ void s_restrict(const SLev& F, const SLev& C) {
 }
 
 // fine x += P x_coarse on fluid fine cells (coarse fluid values only)
-__device__ void s_prolong(const SLev& F, const SLev& C) {
+__device__ void s_prolong(const SLev F, const SLev C) {
     for (int i = threadIdx.x; i < F.n; i += blockDim.x) {
         if (!(F.code[i] & CODE_FLUID)) continue;
         const int z = i % F.nz, y = (i / F.nz) % F.ny, x = i / (F.nz * F.ny);
@@ -1193,8 +1197,10 @@ __device__ void smem_vcycle(const MGChain& C, float* smem) {
         const MGLev& G = C.lev[l];
         const SLev& L = S[l];
         for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
-            const long long gi = (long long)(i / L.nz) * G.pz + (i % L.nz);
-            L.code[i] = G.code[gi];
+            const int z = i % L.nz, t = i / L.nz;
+            const long long gi = (long long)t * G.pz + z;
+            const int odd = (t / L.ny + t % L.ny + z) & 1;
+            L.code[i] = G.code[gi] | (odd ? SCODE_ODD : 0);
             L.x[i] = 0.f;
             if (l == C.ls) L.f[i] = G.f[gi];
         }
