@@ -823,6 +823,11 @@ __device__ __forceinline__ void prolong_quad(const MGLev& F, const MGLev& Cl, in
     const int py = (y & 1) ? y >> 1 : (y >> 1) - 1;
     const float wlx = (x & 1) ? 0.75f : 0.25f, wly = (y & 1) ? 0.75f : 0.25f;
     const int zc = (z0 >> 1) - 1;
+    // coarse z zc .. zc + 3: with h = z0 / 2 even, either the quad at h plus the
+    // value below it (h = 0 mod 4) or the quad at h - 2 plus the value above it
+    const int hq = (z0 >> 1) & ~3;
+    const bool lowq = ((z0 >> 1) & 3) == 0;
+    const int ze = lowq ? zc : hq + 4;  // the extra value's z
     float sum[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int o = 0; o < 4; o++) {
@@ -831,11 +836,20 @@ __device__ __forceinline__ void prolong_quad(const MGLev& F, const MGLev& Cl, in
         if (cx < 0 || cy < 0 || cx >= Cl.nx || cy >= Cl.ny) continue;
         const float wxy = (ox ? 1.f - wlx : wlx) * (oy ? 1.f - wly : wly);
         const long long row = ((long long)cx * Cl.ny + cy) * Cl.pz;
+        float qv[4];
+        uint16_t qc[4];
+        unpack4(ld4(Cl.x + row + hq), qv);
+        codes4(Cl.code, row + hq, qc);
+        const bool ein = ze >= 0 && ze < Cl.pz;
+        const float ev = ein ? Cl.x[row + ze] : 0.f;
+        const uint16_t ec = ein ? Cl.code[row + ze] : (uint16_t)0;
         float cv[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            const int z = zc + k;
-            cv[k] = (z >= 0 && z < Cl.nz && (Cl.code[row + z] & CODE_FLUID)) ? Cl.x[row + z] : 0.f;
+            // lowq: zc = hq - 1 (the extra value), then hq .. hq + 2; else hq + 1 .. hq + 3, then hq + 4
+            const float v = lowq ? (k == 0 ? ev : qv[k - 1]) : (k == 3 ? ev : qv[k + 1]);
+            const uint16_t c = lowq ? (k == 0 ? ec : qc[k - 1]) : (k == 3 ? ec : qc[k + 1]);
+            cv[k] = (c & CODE_FLUID) ? v : 0.f;
         }
         // lanes: z0 (lower zc, w 1/4), z0+1 (zc+1, 3/4), z0+2 (zc+1, 1/4), z0+3 (zc+2, 3/4)
         sum[0] += wxy * (0.25f * cv[0] + 0.75f * cv[1]);
@@ -1083,39 +1097,60 @@ struct SLev {
 
 __device__ __forceinline__ int sidx(const SLev& L, int x, int y, int z) { return (x * L.ny + y) * L.nz + z; }
 
+// Each thread holds at most four cells of a shared-memory level (<= 4096 cells,
+// 1024 threads): a pass computes all of them before it stores any, so their
+// loads overlap (a half sweep's cells read only the other colour)
+constexpr int SCELLS_PER_THREAD = 4;
+static_assert(SCELLS_PER_THREAD * MG_CLUSTER_THREADS >= MG_SMEM_CELLS, "shared-memory level cells per thread");
+
+__device__ __forceinline__ float s_nbsum(const SLev& L, int i, uint16_t cc, int sx, int sy) {
+    float s = 0.f;
+    if (cc & 1) s += L.x[i + sx];
+    if (cc & 2) s += L.x[i - sx];
+    if (cc & 4) s += L.x[i + sy];
+    if (cc & 8) s += L.x[i - sy];
+    if (cc & 16) s += L.x[i + 1];
+    if (cc & 32) s += L.x[i - 1];
+    return s;
+}
+
 __device__ void s_smooth(const SLev L, int color) {
     const int sx = L.ny * L.nz, sy = L.nz;
     const uint16_t want = CODE_FLUID | (color ? SCODE_ODD : 0);
-    for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
+    float nv[SCELLS_PER_THREAD];
+    bool act[SCELLS_PER_THREAD];
+#pragma unroll
+    for (int k = 0; k < SCELLS_PER_THREAD; k++) {
+        const int i = threadIdx.x + k * MG_CLUSTER_THREADS;
+        act[k] = false;
+        nv[k] = 0.f;
+        if (i >= L.n) continue;
         const uint16_t cc = L.code[i];
         if ((cc & (CODE_FLUID | SCODE_ODD)) != want) continue;
-        float s = 0.f;
-        if (cc & 1) s += L.x[i + sx];
-        if (cc & 2) s += L.x[i - sx];
-        if (cc & 4) s += L.x[i + sy];
-        if (cc & 8) s += L.x[i - sy];
-        if (cc & 16) s += L.x[i + 1];
-        if (cc & 32) s += L.x[i - 1];
-        L.x[i] = (L.f[i] + s) * c_rcp[code_ns(cc)];
+        act[k] = true;
+        nv[k] = (L.f[i] + s_nbsum(L, i, cc, sx, sy)) * c_rcp[code_ns(cc)];
     }
+#pragma unroll
+    for (int k = 0; k < SCELLS_PER_THREAD; k++)
+        if (act[k]) L.x[threadIdx.x + k * MG_CLUSTER_THREADS] = nv[k];
     __syncthreads();
 }
 
 __device__ void s_residual(const SLev L) {
-    for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
+    const int sx = L.ny * L.nz, sy = L.nz;
+    float rv[SCELLS_PER_THREAD];
+#pragma unroll
+    for (int k = 0; k < SCELLS_PER_THREAD; k++) {
+        const int i = threadIdx.x + k * MG_CLUSTER_THREADS;
+        rv[k] = 0.f;
+        if (i >= L.n) continue;
         const uint16_t cc = L.code[i];
-        float rv = 0.f;
-        if (cc & CODE_FLUID) {
-            float s = 0.f;
-            if (cc & 1) s += L.x[i + L.ny * L.nz];
-            if (cc & 2) s += L.x[i - L.ny * L.nz];
-            if (cc & 4) s += L.x[i + L.nz];
-            if (cc & 8) s += L.x[i - L.nz];
-            if (cc & 16) s += L.x[i + 1];
-            if (cc & 32) s += L.x[i - 1];
-            rv = L.f[i] - ((float)code_ns(cc) * L.x[i] - s);
-        }
-        L.r[i] = rv;
+        if (cc & CODE_FLUID) rv[k] = L.f[i] - ((float)code_ns(cc) * L.x[i] - s_nbsum(L, i, cc, sx, sy));
+    }
+#pragma unroll
+    for (int k = 0; k < SCELLS_PER_THREAD; k++) {
+        const int i = threadIdx.x + k * MG_CLUSTER_THREADS;
+        if (i < L.n) L.r[i] = rv[k];
     }
     __syncthreads();
 }
@@ -1131,19 +1166,23 @@ __device__ void s_restrict(const SLev F, const SLev C) {
             C.f[i] = 0.f;
             continue;
         }
+        // the fine residual is zero off the fine fluid cells (s_residual)
         float sum = 0.f;
+#pragma unroll
         for (int dx = -1; dx <= 2; dx++) {
             const int fx = 2 * cx + dx;
             if (fx < 0 || fx >= F.nx) continue;
+#pragma unroll
             for (int dy = -1; dy <= 2; dy++) {
                 const int fy = 2 * cy + dy;
                 if (fy < 0 || fy >= F.ny) continue;
                 const float wxy = fw_weight(dx) * fw_weight(dy);
+                const int row = sidx(F, fx, fy, 0);
+#pragma unroll
                 for (int dz = -1; dz <= 2; dz++) {
                     const int fz = 2 * cz + dz;
                     if (fz < 0 || fz >= F.nz) continue;
-                    const int fi = sidx(F, fx, fy, fz);
-                    if (F.code[fi] & CODE_FLUID) sum += wxy * fw_weight(dz) * F.r[fi];
+                    sum += wxy * fw_weight(dz) * F.r[row + fz];
                 }
             }
         }
