@@ -778,14 +778,14 @@ __device__ __forceinline__ void restrict_quad(const MGLev& F, const MGLev& Cl, i
                     const int z = fz0 + 4 * k;
                     float v[4] = {0.f, 0.f, 0.f, 0.f};
                     if (z >= 0 && z < F.pz) {
+                        // codes and residual loaded together; r is stale on quads
+                        // without fluid (never written), so the codes mask it
                         uint16_t fc[4];
                         codes4(F.code, row + z, fc);
-                        if (any_fluid(fc)) {
-                            unpack4(ld4(F.r + row + z), v);
+                        unpack4(ld4(F.r + row + z), v);
 #pragma unroll
-                            for (int e = 0; e < 4; e++)
-                                if (!(fc[e] & CODE_FLUID)) v[e] = 0.f;
-                        }
+                        for (int e = 0; e < 4; e++)
+                            if (!(fc[e] & CODE_FLUID)) v[e] = 0.f;
                     }
 #pragma unroll
                     for (int e = 0; e < 4; e++) fr[4 * k + e] = v[e];
@@ -1074,11 +1074,19 @@ constexpr int MG_CLUSTER_THREADS = 1024;
 // full-GPU launches (35.6 -> 37.5 steps/s); moving the 32^3 level out as well
 // changed nothing.
 constexpr long long MG_CLUSTER_CELLS = 40000;
+constexpr int MG_CLUSTER_SMEM = 200 * 1024;  // dynamic shared memory limit of the cluster kernel
 
 struct MGChain {
     MGLev lev[MG_MAX_LEVELS];
     int lc, last, nu;
     int ls;  // first level small enough to run in one CTA's shared memory (<= last)
+    // levels lc .. ls-1 as x slabs in distributed shared memory (slab != 0):
+    // planes per CTA and float offset of each level in the pool, then the offset
+    // of rank 0's shared-memory levels
+    int slab;
+    int P[MG_MAX_LEVELS];
+    int off[MG_MAX_LEVELS];
+    int soff;
 };
 
 // ---- the smallest levels in one CTA's shared memory ----------------------------
@@ -1213,10 +1221,11 @@ __device__ void s_prolong(const SLev F, const SLev C) {
     __syncthreads();
 }
 
-// V-cycle of chain levels ls..last in the block's shared memory; level ls's rhs
-// comes from global memory, its correction goes back there
-__device__ void smem_vcycle(const MGChain& C, float* smem) {
-    __shared__ SLev S[MG_MAX_LEVELS];
+// Levels ls..last in one CTA's shared memory, dense (z fastest), laid out from
+// `smem` level by level: x, f, r (n floats each), then the codes (n uint16,
+// padded to whole floats).  load_f: level ls's rhs comes from global memory
+// (otherwise the caller's restriction writes it into this layout).
+__device__ void smem_levels_init(const MGChain& C, float* smem, SLev* S, bool load_f) {
     if (threadIdx.x == 0) {
         float* p = smem;
         for (int l = C.ls; l <= C.last; l++) {
@@ -1234,17 +1243,22 @@ __device__ void smem_vcycle(const MGChain& C, float* smem) {
     __syncthreads();
     for (int l = C.ls; l <= C.last; l++) {
         const MGLev& G = C.lev[l];
-        const SLev& L = S[l];
+        const SLev L = S[l];
         for (int i = threadIdx.x; i < L.n; i += blockDim.x) {
             const int z = i % L.nz, t = i / L.nz;
             const long long gi = (long long)t * G.pz + z;
             const int odd = (t / L.ny + t % L.ny + z) & 1;
             L.code[i] = G.code[gi] | (odd ? SCODE_ODD : 0);
             L.x[i] = 0.f;
-            if (l == C.ls) L.f[i] = G.f[gi];
+            if (l == C.ls && load_f) L.f[i] = G.f[gi];
         }
     }
     __syncthreads();
+}
+
+// the V-cycle over those levels; store_x: level ls's correction goes back to
+// global memory (otherwise the caller's prolongation reads it in place)
+__device__ void smem_levels_run(const MGChain& C, const SLev* S, bool store_x) {
     for (int l = C.ls; l < C.last; l++) {
         for (int k = 0; k < C.nu; k++) {
             s_smooth(S[l], 0);
@@ -1268,9 +1282,11 @@ __device__ void smem_vcycle(const MGChain& C, float* smem) {
             s_smooth(S[l], 0);
         }
     }
-    const MGLev& G = C.lev[C.ls];
-    for (int i = threadIdx.x; i < S[C.ls].n; i += blockDim.x)
-        G.x[(long long)(i / S[C.ls].nz) * G.pz + (i % S[C.ls].nz)] = S[C.ls].x[i];
+    if (store_x) {
+        const MGLev& G = C.lev[C.ls];
+        for (int i = threadIdx.x; i < S[C.ls].n; i += blockDim.x)
+            G.x[(long long)(i / S[C.ls].nz) * G.pz + (i % S[C.ls].nz)] = S[C.ls].x[i];
+    }
 }
 
 __device__ __forceinline__ void cluster_barrier() {
@@ -1288,12 +1304,247 @@ __device__ __forceinline__ unsigned cluster_size() {
 }
 
 
+// ---- cluster levels held in distributed shared memory ------------------------
+// With MGChain::slab set, every CTA of the cluster holds P consecutive x planes
+// of each level lc .. ls-1 in its own shared memory (x, f, r and the codes, at
+// the same offsets in every CTA) and reads its neighbours' boundary planes
+// through distributed shared memory; the cluster barrier separates the passes.
+// The restriction into level ls writes straight into rank 0's shared-memory
+// levels, and the prolongation from ls reads them there, so only level lc's
+// rhs comes from global memory and only its correction goes back.
+constexpr uint16_t SCODE_XLO = 0x2000;  // slab copies: x - 1 lies in the previous CTA
+constexpr uint16_t SCODE_XHI = 0x1000;  // slab copies: x + 1 lies in the next CTA
+
+struct DLev {
+    float *x, *f, *r;
+    uint16_t* code;
+    int nx, ny, nz, P, np, x0, plane;
+};
+
+__device__ __forceinline__ DLev dlev(const MGChain& C, int l, float* pool, unsigned rank) {
+    const MGLev& G = C.lev[l];
+    DLev D;
+    D.nx = G.nx; D.ny = G.ny; D.nz = G.nz;
+    D.P = C.P[l];
+    D.plane = G.ny * G.nz;
+    D.x0 = (int)rank * D.P;
+    D.np = max(0, min(D.P, G.nx - D.x0));
+    const int m = D.P * D.plane;
+    float* p = pool + C.off[l];
+    D.x = p;
+    D.f = p + m;
+    D.r = p + 2 * m;
+    D.code = reinterpret_cast<uint16_t*>(p + 3 * m);
+    return D;
+}
+
+// the same shared-memory location in cluster CTA `rank` (generic address)
+template <typename T>
+__device__ __forceinline__ T* dsm(T* p, unsigned rank) {
+    unsigned long long out;
+    asm("mapa.u64 %0, %1, %2;" : "=l"(out) : "l"(reinterpret_cast<unsigned long long>(p)), "r"(rank));
+    return reinterpret_cast<T*>(out);
+}
+
+__device__ __forceinline__ float slab_nbsum(const DLev& D, int i, uint16_t cc, const float* xp, const float* xn) {
+    float s = 0.f;
+    if (cc & 1) s += (cc & SCODE_XHI) ? xn[i - (D.np - 1) * D.plane] : D.x[i + D.plane];
+    if (cc & 2) s += (cc & SCODE_XLO) ? xp[i + (D.P - 1) * D.plane] : D.x[i - D.plane];
+    if (cc & 4) s += D.x[i + D.nz];
+    if (cc & 8) s += D.x[i - D.nz];
+    if (cc & 16) s += D.x[i + 1];
+    if (cc & 32) s += D.x[i - 1];
+    return s;
+}
+
+// red-black half sweep; first: the other colour is still zero
+__device__ void slab_smooth(const DLev& D, int color, bool first, const float* xp, const float* xn) {
+    const uint16_t want = CODE_FLUID | (color ? SCODE_ODD : 0);
+    const int n = D.np * D.plane;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint16_t cc = D.code[i];
+        if ((cc & (CODE_FLUID | SCODE_ODD)) != want) continue;
+        float sum = D.f[i];
+        if (!first) sum += slab_nbsum(D, i, cc, xp, xn);
+        D.x[i] = sum * c_rcp[code_ns(cc)];
+    }
+}
+
+__device__ void slab_residual(const DLev& D, const float* xp, const float* xn) {
+    const int n = D.np * D.plane;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint16_t cc = D.code[i];
+        float rv = 0.f;
+        if (cc & CODE_FLUID) rv = D.f[i] - ((float)code_ns(cc) * D.x[i] - slab_nbsum(D, i, cc, xp, xn));
+        D.r[i] = rv;
+    }
+}
+
+// coarse f = 0.5 * sum_fine P r from level l's slabs (r is zero off the fluid)
+// into level l + 1: the CTA's own slab, or rank 0's first shared-memory level
+// (its cells spread over the whole cluster)
+__device__ void slab_restrict(const MGChain& C, int l, float* pool, unsigned rank, unsigned cs, float* spool) {
+    const DLev F = dlev(C, l, pool, rank);
+    const MGLev& Gc = C.lev[l + 1];
+    const bool to_slab = l + 1 < C.ls;
+    const DLev D = dlev(C, l + 1, pool, rank);  // used only when to_slab
+    const int nsm = Gc.nx * Gc.ny * Gc.nz;
+    const int n = to_slab ? D.np * D.plane : nsm;
+    const int i0 = to_slab ? (int)threadIdx.x : (int)(rank * blockDim.x + threadIdx.x);
+    const int step = to_slab ? (int)blockDim.x : (int)(cs * blockDim.x);
+    float* fout = to_slab ? D.f : dsm(spool + nsm, 0);
+    const uint16_t* cin = to_slab ? D.code : reinterpret_cast<const uint16_t*>(dsm(spool + 3 * nsm, 0));
+    for (int i = i0; i < n; i += step) {
+        int cx, cy, cz;
+        if (to_slab) {
+            const int xl = i / D.plane, t = i - xl * D.plane;
+            cx = D.x0 + xl;
+            cy = t / Gc.nz;
+            cz = t - cy * Gc.nz;
+        } else {
+            cz = i % Gc.nz;
+            const int t = i / Gc.nz;
+            cy = t % Gc.ny;
+            cx = t / Gc.ny;
+        }
+        if (!(cin[i] & CODE_FLUID)) {
+            fout[i] = 0.f;
+            continue;
+        }
+        float sum = 0.f;
+        for (int dx = -1; dx <= 2; dx++) {
+            const int fx = 2 * cx + dx;
+            if (fx < 0 || fx >= F.nx) continue;
+            const unsigned ro = (unsigned)(fx / F.P);
+            const float* rp = (ro == rank ? F.r : dsm(F.r, ro)) + (fx - (int)ro * F.P) * F.plane;
+#pragma unroll
+            for (int dy = -1; dy <= 2; dy++) {
+                const int fy = 2 * cy + dy;
+                if (fy < 0 || fy >= F.ny) continue;
+                const float wxy = fw_weight(dx) * fw_weight(dy);
+                const float* row = rp + fy * F.nz;
+#pragma unroll
+                for (int dz = -1; dz <= 2; dz++) {
+                    const int fz = 2 * cz + dz;
+                    if (fz < 0 || fz >= F.nz) continue;
+                    sum += wxy * fw_weight(dz) * row[fz];
+                }
+            }
+        }
+        fout[i] = 0.5f * sum;
+    }
+}
+
+// fine x += P x_coarse on level l's fluid cells (coarse fluid values only), the
+// coarse level being level l + 1's slabs or rank 0's first shared-memory level
+__device__ void slab_prolong(const MGChain& C, int l, float* pool, unsigned rank, float* spool) {
+    const DLev F = dlev(C, l, pool, rank);
+    const MGLev& Gc = C.lev[l + 1];
+    const bool from_slab = l + 1 < C.ls;
+    const DLev D = dlev(C, l + 1, pool, rank);  // used only when from_slab
+    const int nsm = Gc.nx * Gc.ny * Gc.nz;
+    const float* sx0 = from_slab ? nullptr : dsm(spool, 0);
+    const uint16_t* sc0 = from_slab ? nullptr : reinterpret_cast<const uint16_t*>(dsm(spool + 3 * nsm, 0));
+    const int n = F.np * F.plane;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        if (!(F.code[i] & CODE_FLUID)) continue;
+        const int xl = i / F.plane, t = i - xl * F.plane;
+        const int x = F.x0 + xl, y = t / F.nz, z = t - y * F.nz;
+        const int p[3] = {(x & 1) ? x >> 1 : (x >> 1) - 1, (y & 1) ? y >> 1 : (y >> 1) - 1,
+                          (z & 1) ? z >> 1 : (z >> 1) - 1};
+        const float wl[3] = {(x & 1) ? 0.75f : 0.25f, (y & 1) ? 0.75f : 0.25f, (z & 1) ? 0.75f : 0.25f};
+        float sum = 0.f;
+#pragma unroll
+        for (int o = 0; o < 8; o++) {
+            const int ox = o >> 2, oy = (o >> 1) & 1, oz = o & 1;
+            const int cx = p[0] + ox, cy = p[1] + oy, cz = p[2] + oz;
+            if (cx < 0 || cy < 0 || cz < 0 || cx >= Gc.nx || cy >= Gc.ny || cz >= Gc.nz) continue;
+            float v;
+            uint16_t c;
+            if (from_slab) {
+                const unsigned ro = (unsigned)(cx / D.P);
+                const int li = ((cx - (int)ro * D.P) * Gc.ny + cy) * Gc.nz + cz;
+                v = (ro == rank ? D.x : dsm(D.x, ro))[li];
+                c = (ro == rank ? D.code : dsm(D.code, ro))[li];
+            } else {
+                const int ci = (cx * Gc.ny + cy) * Gc.nz + cz;
+                v = sx0[ci];
+                c = sc0[ci];
+            }
+            if (!(c & CODE_FLUID)) continue;
+            sum += (ox ? 1.f - wl[0] : wl[0]) * (oy ? 1.f - wl[1] : wl[1]) * (oz ? 1.f - wl[2] : wl[2]) * v;
+        }
+        F.x[i] += sum;
+    }
+}
+
 __global__ void __launch_bounds__(MG_CLUSTER_THREADS) k_mg_coarse(const PcgArgs A, const __grid_constant__ MGChain C) {
     pdl_enter();
     if (A.st->done) return;  // the same value in every CTA of the cluster
     extern __shared__ float pool[];
-    const long long i0 = (long long)cluster_rank() * blockDim.x + threadIdx.x;
-    const long long step = (long long)cluster_size() * blockDim.x;
+    __shared__ SLev S[MG_MAX_LEVELS];
+    const unsigned rank = cluster_rank(), cs = cluster_size();
+    if (C.slab) {
+        float* spool = pool + C.soff;
+        for (int l = C.lc; l < C.ls; l++) {
+            const DLev D = dlev(C, l, pool, rank);
+            const MGLev& G = C.lev[l];
+            for (int i = threadIdx.x; i < D.np * D.plane; i += blockDim.x) {
+                const int xl = i / D.plane, t = i - xl * D.plane, y = t / D.nz, z = t - y * D.nz;
+                const long long gi = ((long long)(D.x0 + xl) * G.ny + y) * G.pz + z;
+                uint16_t cc = G.code[gi];
+                if ((D.x0 + xl + y + z) & 1) cc |= SCODE_ODD;
+                if (xl == 0) cc |= SCODE_XLO;
+                if (xl == D.np - 1) cc |= SCODE_XHI;
+                D.code[i] = cc;
+                D.x[i] = 0.f;
+                if (l == C.lc) D.f[i] = G.f[gi];
+            }
+        }
+        if (rank == 0) smem_levels_init(C, spool, S, false);
+        cluster_barrier();
+        for (int l = C.lc; l < C.ls; l++) {
+            const DLev D = dlev(C, l, pool, rank);
+            const float* xp = rank > 0 ? dsm(D.x, rank - 1) : nullptr;
+            const float* xn = rank + 1 < cs ? dsm(D.x, rank + 1) : nullptr;
+            for (int k = 0; k < C.nu; k++) {
+                slab_smooth(D, 0, k == 0, xp, xn);
+                cluster_barrier();
+                slab_smooth(D, 1, false, xp, xn);
+                cluster_barrier();
+            }
+            slab_residual(D, xp, xn);
+            cluster_barrier();
+            slab_restrict(C, l, pool, rank, cs, spool);
+            cluster_barrier();
+        }
+        if (rank == 0) smem_levels_run(C, S, false);
+        cluster_barrier();
+        for (int l = C.ls - 1; l >= C.lc; l--) {
+            const DLev D = dlev(C, l, pool, rank);
+            const float* xp = rank > 0 ? dsm(D.x, rank - 1) : nullptr;
+            const float* xn = rank + 1 < cs ? dsm(D.x, rank + 1) : nullptr;
+            slab_prolong(C, l, pool, rank, spool);
+            cluster_barrier();
+            for (int k = 0; k < C.nu; k++) {
+                slab_smooth(D, 1, false, xp, xn);
+                cluster_barrier();
+                slab_smooth(D, 0, false, xp, xn);
+                cluster_barrier();
+            }
+        }
+        // level lc's correction back to global memory (its slab alone: no other
+        // CTA reads this CTA's shared memory after the last barrier)
+        const DLev D = dlev(C, C.lc, pool, rank);
+        const MGLev& G = C.lev[C.lc];
+        for (int i = threadIdx.x; i < D.np * D.plane; i += blockDim.x) {
+            const int xl = i / D.plane, t = i - xl * D.plane, y = t / D.nz, z = t - y * D.nz;
+            G.x[((long long)(D.x0 + xl) * G.ny + y) * G.pz + z] = D.x[i];
+        }
+        return;
+    }
+    const long long i0 = (long long)rank * blockDim.x + threadIdx.x;
+    const long long step = (long long)cs * blockDim.x;
     for (int l = C.lc; l < C.ls; l++) {
         const MGLev& L = C.lev[l];
         for (int k = 0; k < C.nu; k++) {
@@ -1308,7 +1559,10 @@ __global__ void __launch_bounds__(MG_CLUSTER_THREADS) k_mg_coarse(const PcgArgs 
         mg_for_range(Cl, i0, step, [&](int x, int y, int z0, long long c0) { restrict_quad(L, Cl, x, y, z0, c0); });
         cluster_barrier();
     }
-    if (cluster_rank() == 0) smem_vcycle(C, pool);
+    if (rank == 0) {
+        smem_levels_init(C, pool, S, true);
+        smem_levels_run(C, S, true);
+    }
     cluster_barrier();
     for (int l = C.ls - 1; l >= C.lc; l--) {
         const MGLev& L = C.lev[l];
@@ -1463,7 +1717,7 @@ int solver_alloc(fsim_ctx* ctx) {
     }
     // cluster for the coarse V-cycle: 16 CTAs where the GPU schedules them, else 8
     S.mg_cluster = 0;
-    cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, MG_CLUSTER_SMEM);
     for (int cs : {16, 8}) {
         if (cs > 8 && cudaFuncSetAttribute(k_mg_coarse, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
                           cudaSuccess) {
@@ -1473,6 +1727,7 @@ int solver_alloc(fsim_ctx* ctx) {
         cudaLaunchConfig_t cfg{};
         cfg.gridDim = dim3(cs);
         cfg.blockDim = dim3(MG_CLUSTER_THREADS);
+        cfg.dynamicSmemBytes = MG_CLUSTER_SMEM;  // the most a launch asks for
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
         at[0].val.clusterDim.x = cs;
@@ -1559,10 +1814,24 @@ static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, c
             const long long n = (long long)b.nx * b.ny * b.nz;
             smem += (size_t)(3 * n + (n + 1) / 2) * sizeof(float);
         }
+        // levels lc .. ls-1 as x slabs in the cluster's distributed shared memory
+        // when they fit beside rank 0's levels (else they run in global memory)
+        size_t slab_floats = 0;
+        for (int k = 0; k < C.ls; k++) {
+            const MGLevelBufs& b = S.mg[l + k];
+            const int P = ceil_div(b.nx, S.mg_cluster);
+            const long long m = (long long)P * b.ny * b.nz;
+            C.P[k] = P;
+            C.off[k] = (int)slab_floats;
+            slab_floats += (size_t)((3 * m + (m + 1) / 2 + 3) & ~3ll);
+        }
+        C.soff = (int)slab_floats;
+        const size_t slab_bytes = slab_floats * sizeof(float) + smem;
+        C.slab = (C.ls > 0 && slab_bytes <= (size_t)MG_CLUSTER_SMEM) ? 1 : 0;
         cudaLaunchConfig_t cfg{};
         cfg.gridDim = dim3(S.mg_cluster);
         cfg.blockDim = dim3(MG_CLUSTER_THREADS);
-        cfg.dynamicSmemBytes = smem;
+        cfg.dynamicSmemBytes = C.slab ? slab_bytes : smem;
         cfg.stream = st;
         cudaLaunchAttribute at[2];
         at[0].id = cudaLaunchAttributeClusterDimension;

@@ -140,12 +140,15 @@ def test_full_step_with_push_apart(gpu, port_lib, transfer):
         assert dv < 1e-3, f"step {s}: velocity error {dv}"
 
 
-def test_multigrid_needs_far_fewer_iterations(gpu, port_lib):
-    """Both preconditioners reach the same pressure; multigrid in far fewer iterations."""
-    pos, vel, c = moving_state(32, N.FLIP)
+@pytest.mark.parametrize("res", [32, 64, 96])
+def test_multigrid_needs_far_fewer_iterations(gpu, port_lib, res):
+    """Both preconditioners reach the same pressure; multigrid in far fewer
+    iterations.  At 64^3 and 96^3 the 32^3 / 24^3 level runs as x slabs in the
+    cluster's distributed shared memory (at 96^3 some CTAs hold no plane)."""
+    pos, vel, c = moving_state(res, N.FLIP)
     result = {}
     for precond in (N.PRECOND_RBIC, N.PRECOND_MG):
-        g, o = make_pair(pos, 32, N.FLIP, vel=vel, gpu_tol=1e-8, gpu_tol_mode=N.TOL_REL_L2, gpu_max_iters=3000,
+        g, o = make_pair(pos, res, N.FLIP, vel=vel, gpu_tol=1e-8, gpu_tol_mode=N.TOL_REL_L2, gpu_max_iters=3000,
                          precond=precond)
         g.stage(N.STAGE_P2G, DT32)
         for st in (N.STAGE_OBSTACLES, N.STAGE_WALLS, N.STAGE_POST_P2G):
