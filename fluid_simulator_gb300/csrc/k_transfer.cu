@@ -395,34 +395,56 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
             }
             // shared-box coordinates of the stencil corner
             const int sx = b[0] - (x0 - 1), sy = b[1] - (y0 - 1), sz = b[2] - (z0 - 4);
+            // 1D weights and trilinearInterpollGradient signs (util/interpolation.h:21-35)
+            // of the two nodes per dimension
+            float w1[3][2], sg[3][2];
+#pragma unroll
+            for (int dd = 0; dd < 3; dd++)
+#pragma unroll
+                for (int o = 0; o < 2; o++) {
+                    const float d = d0[dd] - o;
+                    w1[dd][o] = 1.f - fabsf(d);
+                    sg[dd][o] = d > 0.f ? -1.f : 1.f;
+                }
+            if (MODE == 2 && a.g.two_d) {
+                // 2D particles sit on the z node plane, where the sign flips: take it
+                // from the FP64 offset as the reference does (0.15f * 10 rounds to
+                // exactly 1.5 in FP32, 6e-8 above it in FP64)
+#pragma unroll
+                for (int o = 0; o < 2; o++) {
+                    const double e =
+                        ((double)pz - ((double)(b[2] + o) + (ax == 2 ? 1.0 : 0.5)) * a.g.hzd) * a.g.hzinvd;
+                    sg[2][o] = e > 0.0 ? -1.f : 1.f;
+                }
+            }
+            // corner weight (wx wy) wz; a gradient term sign * wy * wz / h equals
+            // sign * ((wy wz) / h) exactly (rounding is symmetric in the sign), so the
+            // four magnitudes per component are formed once per axis
+            float wxy[2][2], gmx[2][2], gmy[2][2], gmz[2][2];
+#pragma unroll
+            for (int i2 = 0; i2 < 2; i2++)
+#pragma unroll
+                for (int j2 = 0; j2 < 2; j2++) {
+                    wxy[i2][j2] = w1[0][i2] * w1[1][j2];
+                    if (MODE == 2) {
+                        gmx[i2][j2] = (w1[1][i2] * w1[2][j2]) * hinv;  // (oy, oz)
+                        gmy[i2][j2] = (w1[0][i2] * w1[2][j2]) * hinv;  // (ox, oz)
+                        gmz[i2][j2] = wxy[i2][j2] * hzinv;             // (ox, oy)
+                    }
+                }
             float pic = 0.f, flip = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
 #pragma unroll
             for (int o = 0; o < 8; o++) {
                 const int ox = o >> 2, oy = (o >> 1) & 1, oz = o & 1;
-                const float dx = d0[0] - ox, dy = d0[1] - oy, dz = d0[2] - oz;
-                const float wx = 1.f - fabsf(dx), wy = 1.f - fabsf(dy), wz = 1.f - fabsf(dz);
-                const float w = wx * wy * wz;
+                const float w = wxy[ox][oy] * w1[2][oz];
                 const int si = ((sx + ox) * BY + (sy + oy)) * BZ + (sz + oz);
                 const float v2 = sv2[ax * BOXN + si];
                 pic += v2 * w;
                 if (MODE == 1) flip += (v2 - su[ax * BOXN + si]) * w;
                 if (MODE == 2) {
-                    // trilinearInterpollGradient (util/interpolation.h:21-35)
-                    float sz_ = dz > 0.f ? -1.f : 1.f;
-                    if (a.g.two_d) {
-                        // 2D particles sit on the z node plane, where the sign flips: take it
-                        // from the FP64 offset as the reference does (0.15f * 10 rounds to
-                        // exactly 1.5 in FP32, 6e-8 above it in FP64)
-                        const double e = ((double)pz - ((double)(b[2] + oz) + (ax == 2 ? 1.0 : 0.5)) * a.g.hzd) *
-                                         a.g.hzinvd;
-                        sz_ = e > 0.0 ? -1.f : 1.f;
-                    }
-                    const float gx = (dx > 0.f ? -1.f : 1.f) * wy * wz * hinv;
-                    const float gy = (dy > 0.f ? -1.f : 1.f) * wx * wz * hinv;
-                    const float gz = sz_ * wx * wy * hzinv;
-                    c0 += gx * v2;
-                    c1 += gy * v2;
-                    c2 += gz * v2;
+                    c0 += (sg[0][ox] * gmx[oy][oz]) * v2;
+                    c1 += (sg[1][oy] * gmy[ox][oz]) * v2;
+                    c2 += (sg[2][oz] * gmz[ox][oy]) * v2;
                 }
             }
             if (MODE == 0) vnew[ax] = pic;
