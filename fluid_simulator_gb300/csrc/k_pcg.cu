@@ -655,14 +655,16 @@ __device__ __forceinline__ long long lev_sx(const MGLev& L) { return (long long)
 // one red-black Gauss-Seidel half sweep of a quad; first: the other colour is still zero
 __device__ __forceinline__ void smooth_quad(const MGLev& L, const float* rhs, int color, int first, int x, int y,
                                             int z0, long long c0) {
+    // every load is issued before the fluid test (one round trip, not two; the
+    // levels sit in L2, so the loads of quads without fluid are cheap)
     uint16_t cc[4];
     codes4(L.code, c0, cc);
-    if (!any_fluid(cc)) return;
     float f[4];
     unpack4(ld4(rhs + c0), f);
     Q7 q;
     if (first) unpack4(ld4(L.x + c0), q.c);
     else load_q7(q, L.x, c0, L, x, y, z0);
+    if (!any_fluid(cc)) return;
     const int par = (x + y + z0) & 1;
     float out[4] = {q.c[0], q.c[1], q.c[2], q.c[3]};
 #pragma unroll
@@ -733,11 +735,11 @@ __global__ void __launch_bounds__(PCG_THREADS) k_mg_smooth_dot(const PcgArgs A, 
 __device__ __forceinline__ void residual_quad(const MGLev& L, const float* rhs, int x, int y, int z0, long long c0) {
     uint16_t cc[4];
     codes4(L.code, c0, cc);
-    if (!any_fluid(cc)) return;
     float f[4];
     unpack4(ld4(rhs + c0), f);
     Q7 q;
     load_q7(q, L.x, c0, L, x, y, z0);
+    if (!any_fluid(cc)) return;
     float out[4];
 #pragma unroll
     for (int i = 0; i < 4; i++)
