@@ -171,7 +171,7 @@ BYTES_PCG_PER_FLUID_CELL_ITER = 60
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one k_p2g / k_g2p launch per
 # particle, from full ncu captures of the same scene at 128^3 (8.0M particles; cells per particle
 # are the same at 256^3, so the per-particle figure scales to the 256^3 launch)
-DRAM_BYTES_PER_PARTICLE = {"p2g": (667.412992e6 + 29.150208e6) / 7999554,
+DRAM_BYTES_PER_PARTICLE = {"p2g": (679.849984e6 + 32.129536e6) / 7999554,
                            "g2p": (170.228736e6 + 425.340672e6) / 7999554}
 
 

@@ -44,13 +44,18 @@ struct P2GArgs {
     int ntx, nty, ntz;
 };
 
-// P2G tile (owned cells) and its one-cell halo: 12x16x16 owned cells, seven
+// P2G tile (owned cells) and its one-cell halo: 8x16x16 owned cells, seven
 // FP32 shared accumulators per cell (face v and weight per axis, density) =
-// 86 KB, so two 384-thread CTAs fit on an SM
-constexpr int PX = 12, PY = 16, PZ = 16;
+// 57 KB, two 384-thread CTAs per SM.  Tile shapes measured on the 256^3 APIC
+// workload (kernel ms): 8x16x16 4.56, 6x16x16 4.71, 12x12x12 4.73,
+// 12x16x16 4.75, 8x12x24 4.79, 8x8x32 4.83, 16x16x8 4.96, 8x16x24 5.03.  A
+// tile narrow in x (the slowest axis of the cell order) spans fewer runs of
+// sorted particles, and the smaller shared-memory share leaves L1 more room
+// for the particle re-reads of the four warp roles.
+constexpr int PX = 8, PY = 16, PZ = 16;
 constexpr int QX = PX + 2, QY = PY + 2, QZ = PZ + 2;
 constexpr int PCELLS = PX * PY * PZ;
-constexpr int P2G_SMEM = 7 * PCELLS * (int)sizeof(float);  // 86,016 B
+constexpr int P2G_SMEM = 7 * PCELLS * (int)sizeof(float);  // 57,344 B
 constexpr int P2G_THREADS = 384;
 
 // 1D tent weights of the three cell-centred nodes at relative -0.5, 0.5, 1.5
@@ -72,7 +77,7 @@ __device__ __forceinline__ void tent3(float f, float (&w)[3]) {
 // contribution of all particles of the cell, at most 36 registers -- then adds
 // the entries inside the tile to the tile's shared accumulators (lanes hold
 // distinct cells, so a warp's adds never collide).  Measured on the 256^3 APIC
-// workload (before the one-ahead loads below): 5.33 ms, against 5.69 ms for warp
+// workload (12x16x16 tiles, before the one-ahead loads below): 5.33 ms, against 5.69 ms for warp
 // pairs (x + density / y + z, 72 accumulators, 168 registers, a 12x16x32 tile
 // and one CTA per SM).
 template <bool APIC, int AX, int OW, int OV, int NA>
