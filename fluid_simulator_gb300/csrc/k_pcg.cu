@@ -529,9 +529,13 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
 // residual, far below a 10^-3 drop.  One decade per fold (the first setting)
 // cost 5 refinements per 1e-6 solve at 256^3.
 constexpr int MIXED_REFINE_DIGITS = 3;
+// Per-level defaults re-measured on the 256^3 fill workload (steps/s, level 1 /
+// deeper separate levels / cluster levels): 4/6/8 45.2, 4/8/6 45.0, 6/4/6 45.0,
+// 5/5/8 44.9, 4/4/8 44.7 (18 iterations), 6/6/6 44.4, 4/8/10 44.0, 6/6/4 43.6.
 constexpr int MG_NU_DEFAULT = 2;           // level 0
-constexpr int MG_NU_COARSE_DEFAULT = 6;    // level 1 and other separately launched levels
-constexpr int MG_NU_CLUSTER_DEFAULT = 6;   // levels run by the cluster kernel
+constexpr int MG_NU_L1_DEFAULT = 4;        // level 1 (128^3 at 256^3)
+constexpr int MG_NU_COARSE_DEFAULT = 6;    // deeper separately launched levels
+constexpr int MG_NU_CLUSTER_DEFAULT = 8;   // levels run by the cluster kernel
 constexpr int MG_BOTTOM_SWEEPS = 4;  // on the <= 4^3 bottom level; 12 gave the same iterations, 12 us/it slower
 constexpr int MG_BOTTOM_MAX = 4096;
 
@@ -1785,7 +1789,7 @@ static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, c
     const int NU0 = P.mg_sweeps > 0 ? P.mg_sweeps : MG_NU_DEFAULT;
     const int NU1 = P.mg_coarse_sweeps > 0 ? P.mg_coarse_sweeps : MG_NU_COARSE_DEFAULT;
     const int NUC = P.mg_cluster_sweeps > 0 ? P.mg_cluster_sweeps : MG_NU_CLUSTER_DEFAULT;
-    const int NU = l == 0 ? NU0 : NU1;
+    const int NU = l == 0 ? NU0 : (P.mg_coarse_sweeps > 0 ? NU1 : (l == 1 ? MG_NU_L1_DEFAULT : NU1));
     SolverBufs& S = ctx->sv;
     cudaStream_t st = ctx->stream;
     const int G = S.grid_blocks;

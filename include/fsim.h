@@ -169,8 +169,9 @@ typedef struct fsim_params {
     int precond;            /* fsim_precond (FSIM_PREC_FP64 always uses FSIM_PRECOND_RBIC) */
     int mg_sweeps;          /* multigrid smoothing sweeps before and after the coarse correction on
                                the finest level (0: 2) */
-    int mg_coarse_sweeps;   /* the same on level 1 and other levels run as separate kernels (0: 6) */
-    int mg_cluster_sweeps;  /* the same on the small levels run by one thread-block cluster (0: 6) */
+    int mg_coarse_sweeps;   /* the same on level 1 and other levels run as separate kernels (0: 4 on
+                               level 1, 6 below it) */
+    int mg_cluster_sweeps;  /* the same on the small levels run by one thread-block cluster (0: 8) */
     int grid_solver;        /* fsim_grid_solver: SimulationConfig::gridSolverType */
     int learned_backoff;    /* FSIM_WARM_LEARNED: after a rejected network guess skip the network on
                                the next 1, 2, 4 ... 64 solves (previous pressure instead); 0: judge
