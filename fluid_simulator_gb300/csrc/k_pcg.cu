@@ -267,6 +267,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_residual(const PcgArgs a, Vecs<
     __shared__ double scratch[32 * 4];
     T* r = (a.st->bufsel & 1) ? v.r[1] : v.r[0];
     double acc[4] = {0.0, -1e300, 0.0, -1e300};  // rr, rmax, bb, bmax
+    T rmaxT = (T)0;
     const int nact = *a.nactive;
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int x, y, z;
@@ -284,13 +285,19 @@ __global__ void __launch_bounds__(PCG_THREADS) k_residual(const PcgArgs a, Vecs<
         }
         const double bc = a.b[c];
         const double rv = bc - ap;
-        r[c] = (T)rv;
+        const T rt = (T)rv;
+        r[c] = rt;
         if (reset_x && sizeof(T) == 4) v.x[c] = (T)0;
+        // FP64 runs at a small fraction of FP32 here: the max norms come from the
+        // stored residual, and the rhs norms are needed by the first residual only
         acc[0] += rv * rv;
-        acc[1] = fmax(acc[1], fabs(rv));
-        acc[2] += bc * bc;
-        acc[3] = fmax(acc[3], fabs(bc));
+        rmaxT = fmax(rmaxT, fabs(rt));
+        if (first) {
+            acc[2] += bc * bc;
+            acc[3] = fmax(acc[3], fabs(bc));
+        }
     }
+    acc[1] = fmax(acc[1], (double)rmaxT);
     if (last_block_reduce<4>(acc, 0xA, a.partials, a.counter, scratch)) {
         if (threadIdx.x == 0) {
             PcgState* s = a.st;
