@@ -64,8 +64,8 @@ __global__ void k_fill_u8(uint8_t* p, long long n, uint8_t v) {
 __global__ void k_init_flags(GridGeom g, int top_solid, uint8_t* f) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.ncell) return;
-    const int z = (int)(c % g.pz);
-    const int y = (int)((c / g.pz) % g.ny), x = (int)(c / ((long long)g.pz * g.ny));
+    int x, y, z;
+    cell_xyz(g, c, x, y, z);
     bool solid = z >= g.nz || x == 0 || x == g.nx - 1 || y == 0 || (top_solid && y == g.ny - 1) || z == 0 ||
                  z == g.nz - 1;
     f[c] = solid ? C_SOLID : C_AIR;
@@ -404,6 +404,14 @@ int fsim_create(const fsim_grid_desc* gd, const fsim_params* params, fsim_ctx** 
     g.hzinvd = 1.0 / g.hzd;
     g.hz = (float)g.hzd;
     g.hzinv = (float)g.hzinvd;
+    // the padded grid stays below 2^31 cells (32-bit cell coordinates in the
+    // kernels; far above what the particle state of such a grid would need)
+    const double cells = std::floor(gd->dims[0] / g.hd) * std::floor(gd->dims[1] / g.hd) *
+                         (g.two_d ? 4.0 : std::floor(gd->dims[2] / g.hd) + 3.0);
+    if (!(cells < 2147483648.0)) {
+        delete ctx;
+        return FSIM_E_INVALID;
+    }
     g.nx = (int)(gd->dims[0] / g.hd);
     g.ny = (int)(gd->dims[1] / g.hd);
     g.nz = g.two_d ? 3 : (int)(gd->dims[2] / g.hd);

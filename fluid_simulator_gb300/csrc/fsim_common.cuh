@@ -59,6 +59,17 @@ __host__ __device__ inline long long gidx(const GridGeom& g, int x, int y, int z
     return ((long long)x * g.ny + y) * g.pz + z;
 }
 
+// (x, y, z) of padded cell c in 32-bit arithmetic (64-bit division is emulated
+// in software on the GPU; fsim_create keeps the padded grid below 2^31 cells)
+__device__ __forceinline__ void cell_xyz(const GridGeom& g, long long c, int& x, int& y, int& z) {
+    const unsigned cu = (unsigned)c, pz = (unsigned)g.pz, ny = (unsigned)g.ny;
+    const unsigned t = cu / pz;
+    z = (int)(cu - t * pz);
+    const unsigned u = t / ny;
+    y = (int)(t - u * ny);
+    x = (int)u;
+}
+
 // SoA particle storage: 16 arrays of `cap` words each.
 struct ParticleBuf {
     float* p[3];    // position

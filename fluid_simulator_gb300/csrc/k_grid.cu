@@ -84,9 +84,9 @@ __global__ void k_prep(GridGeom g, int top_solid, int walls, int post, float gin
                        float* u0, float* u1, float* u2, float* w0, float* w1, float* w2) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.ncell) return;
-    const int z = (int)(c % g.pz);
+    int x, y, z;
+    cell_xyz(g, c, x, y, z);
     if (z >= g.nz) return;
-    const int y = (int)((c / g.pz) % g.ny), x = (int)(c / ((long long)g.pz * g.ny));
     const bool bc = is_border(g, top_solid, x, y, z);
     uint8_t fc = flags[c];
     if (walls && bc) fc = C_SOLID;
@@ -130,9 +130,9 @@ __global__ void k_extrapolate(GridGeom g, int it, const uint8_t* flags, uint8_t*
                               float* v1, float* v2) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.ncell) return;
-    const int z = (int)(c % g.pz);
+    int x, y, z;
+    cell_xyz(g, c, x, y, z);
     if (z >= g.nz) return;
-    const int y = (int)((c / g.pz) % g.ny), x = (int)(c / ((long long)g.pz * g.ny));
     auto vld = [&](long long cc) -> int {
         return it == 0 ? (flags[cc] == C_WATER ? 0 : 100) : valid[cc];
     };
@@ -210,9 +210,9 @@ __global__ void k_apply_pressure(GridGeom g, const uint8_t* flags, const double*
                                  float* v0, float* v1, float* v2) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.ncell) return;
-    const int z = (int)(c % g.pz);
+    int x, y, z;
+    cell_xyz(g, c, x, y, z);
     if (z >= g.nz) return;
-    const int y = (int)((c / g.pz) % g.ny), x = (int)(c / ((long long)g.pz * g.ny));
     const uint8_t fc = flags[c];
     if (fc == C_SOLID) return;
     const long long st[3] = {(long long)g.pz * g.ny, g.pz, 1};

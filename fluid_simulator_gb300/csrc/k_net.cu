@@ -417,8 +417,8 @@ __global__ void k_guess_out(GridGeom g, const uint16_t* code, const float* out, 
                             int W, float* guess) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= g.ncell) return;
-    const int z = (int)(c % g.pz);
-    const int y = (int)((c / g.pz) % g.ny), x = (int)(c / ((long long)g.pz * g.ny));
+    int x, y, z;
+    cell_xyz(g, c, x, y, z);
     float p = 0.f;
     if (z < g.nz && (code[c] & CODE_FLUID_BIT)) p = (float)(out[((long long)x * H + y) * W + z] * rhs_rms(acc));
     guess[c] = p;

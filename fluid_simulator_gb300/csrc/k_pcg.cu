@@ -171,9 +171,9 @@ __global__ void k_setup(const SetupArgs a) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const GridGeom& g = a.B.g;
     if (c >= g.ncell) return;
-    const int z = (int)(c % g.pz);
+    int x, y, z;
+    cell_xyz(g, c, x, y, z);
     if (z >= g.nz) return;
-    const int y = (int)((c / g.pz) % g.ny), x = (int)(c / ((long long)g.pz * g.ny));
     const uint8_t f = a.flags[c];
     if (f != C_WATER || x == 0 || y == 0 || z == 0 || x == g.nx - 1 || y == g.ny - 1 || z == g.nz - 1) {
         a.code[c] = 0;

@@ -30,6 +30,7 @@ def test_create_rejects_bad_grid_and_params():
     assert _create(lib, res=0.0)[0] == -1
     assert _create(lib, dims=(1.0, -1.0, 1.0))[0] == -1
     assert _create(lib, res=2.0)[0] == -1          # fewer than 3 cells per axis
+    assert _create(lib, res=1.0, dims=(2048.0, 2048.0, 1024.0))[0] == -1  # 2^32 cells
     assert _create(lib, transfer=7)[0] == -1        # no such P2G2PType
     assert _create(lib, tol_mode=9)[0] == -1
     assert _create(lib, fluid_density=0.0)[0] == -1
