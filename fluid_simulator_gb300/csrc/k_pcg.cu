@@ -542,7 +542,9 @@ constexpr int MIXED_REFINE_DIGITS = 3;
 constexpr int MG_NU_DEFAULT = 2;           // level 0
 constexpr int MG_NU_L1_DEFAULT = 4;        // level 1 (128^3 at 256^3)
 constexpr int MG_NU_COARSE_DEFAULT = 6;    // deeper separately launched levels
-constexpr int MG_NU_CLUSTER_DEFAULT = 8;   // levels run by the cluster kernel
+constexpr int MG_NU_CLUSTER_DEFAULT = 8;   // cluster levels in global or distributed shared memory
+constexpr int MG_NU_SMALL_DEFAULT = 6;     // levels rank 0 runs alone (<= 4096 cells): 8/6 45.5, 8/8 45.2,
+                                           // 10/6 45.3, 12/4 45.3, 8/4 45.0 (17.75 iterations)
 constexpr int MG_BOTTOM_SWEEPS = 4;  // on the <= 4^3 bottom level; 12 gave the same iterations, 12 us/it slower
 constexpr int MG_BOTTOM_MAX = 4096;
 
@@ -1092,6 +1094,7 @@ constexpr int MG_CLUSTER_SMEM = 200 * 1024;  // dynamic shared memory limit of t
 struct MGChain {
     MGLev lev[MG_MAX_LEVELS];
     int lc, last, nu;
+    int nu_small;  // sweeps on the shared-memory levels ls .. last-1
     int ls;  // first level small enough to run in one CTA's shared memory (<= last)
     // levels lc .. ls-1 as x slabs in distributed shared memory (slab != 0):
     // planes per CTA and float offset of each level in the pool, then the offset
@@ -1273,7 +1276,7 @@ __device__ void smem_levels_init(const MGChain& C, float* smem, SLev* S, bool lo
 // global memory (otherwise the caller's prolongation reads it in place)
 __device__ void smem_levels_run(const MGChain& C, const SLev* S, bool store_x) {
     for (int l = C.ls; l < C.last; l++) {
-        for (int k = 0; k < C.nu; k++) {
+        for (int k = 0; k < C.nu_small; k++) {
             s_smooth(S[l], 0);
             s_smooth(S[l], 1);
         }
@@ -1290,7 +1293,7 @@ __device__ void smem_levels_run(const MGChain& C, const SLev* S, bool store_x) {
     }
     for (int l = C.last - 1; l >= C.ls; l--) {
         s_prolong(S[l], S[l + 1]);
-        for (int k = 0; k < C.nu; k++) {
+        for (int k = 0; k < C.nu_small; k++) {
             s_smooth(S[l], 1);
             s_smooth(S[l], 0);
         }
@@ -1813,6 +1816,7 @@ static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, c
         C.lc = 0;
         C.last = last - l;
         C.nu = NUC;
+        C.nu_small = P.mg_cluster_sweeps > 0 ? NUC : MG_NU_SMALL_DEFAULT;
         // the levels from ls on run in shared memory (x, f, r floats + codes per cell)
         C.ls = C.last;
         size_t smem = 0;

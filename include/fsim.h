@@ -171,7 +171,8 @@ typedef struct fsim_params {
                                the finest level (0: 2) */
     int mg_coarse_sweeps;   /* the same on level 1 and other levels run as separate kernels (0: 4 on
                                level 1, 6 below it) */
-    int mg_cluster_sweeps;  /* the same on the small levels run by one thread-block cluster (0: 8) */
+    int mg_cluster_sweeps;  /* the same on the small levels run by one thread-block cluster (0: 8 on
+                               the cluster-wide levels, 6 on those one CTA runs alone) */
     int grid_solver;        /* fsim_grid_solver: SimulationConfig::gridSolverType */
     int learned_backoff;    /* FSIM_WARM_LEARNED: after a rejected network guess skip the network on
                                the next 1, 2, 4 ... 64 solves (previous pressure instead); 0: judge
