@@ -2,8 +2,8 @@
  * fsim_oracle.c -- CPU oracle: an FP64 plain-C restatement of the reference's
  * per-step simulation path (dkiovics/fluid_simulator, src/Simulator/simulator).
  *
- * TEST INFRASTRUCTURE ONLY.  It is the checker for the CUDA path (tests,
- * __graft_entry__.smoke) and the timed CPU baseline of bench.py; the product
+ * TEST INFRASTRUCTURE ONLY.  The CUDA path's tests and __graft_entry__.smoke
+ * compare against it, and bench.py times it as the CPU baseline; the product
  * never links or calls it.  It follows the reference operation by operation
  * (same expression order, separately rounded FP64 multiplies and adds), so with
  * one thread it reproduces the reference bit for bit; tests/test_oracle_golden.py
@@ -1104,7 +1104,7 @@ static void stage_g2p(sim *s) {
     }
 }
 
-/* ------------------------------------------------------------- driver */
+/* ----------------------------------------------------- stage stepping */
 
 int oracle_stage(void *h, int stage, double dt) {
     sim *s = (sim *)h;

@@ -1,4 +1,4 @@
-"""ctypes driver for the CPU oracles (test infrastructure only).
+"""ctypes bindings of the CPU oracles (test infrastructure only).
 
 Two libraries export the interface declared in ``oracle_api.h``:
 

@@ -42,7 +42,7 @@ def _gpu_available() -> bool:
 
 @pytest.fixture(scope="session")
 def gpu():
-    """The built CUDA library; GPU tests fail (not skip) when it cannot load on a GPU machine."""
+    """The built CUDA library; GPU tests fail (not skip) when it cannot load on a machine with a GPU."""
     if not _gpu_available():
         pytest.skip("no CUDA device visible")
     from fluid_simulator_gb300 import _build, native
