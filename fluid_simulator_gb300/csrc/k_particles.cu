@@ -440,26 +440,56 @@ __global__ void k_spawn_disc(ParticleBuf p, long long first, int ncells, const i
 
 // SimulationManager gfx publish (simulationManager.cpp:218-231): position,
 // |v| and the trilinear interpolation of avgPNum at the particle.
-__global__ void k_gfx(ParticleBuf p, long long n, const float* avg, GridGeom g, fsim_particle_gfx* out) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float px = p.p[0][i], py = p.p[1][i], pz = p.p[2][i];
-    const float vx = p.v[0][i], vy = p.v[1][i], vz = p.v[2][i];
-    const float gx = px * g.hinv - 0.5f, gy = py * g.hinv - 0.5f, gz = pz * g.hzinv - 0.5f;
-    const int bx = (int)gx, by = (int)gy, bz = (int)gz;
-    float dens = 0.f;
+constexpr int GFX_THREADS = 256;
+
+// One 20-byte record per particle.  vec (out 16-byte aligned): the block's
+// records are staged in shared memory and written as contiguous 16-byte
+// stores (a block's records start at 256 * 20 bytes, a multiple of 16), not
+// as five 4-byte stores at a 20-byte stride per lane.
+__global__ void __launch_bounds__(GFX_THREADS) k_gfx(ParticleBuf p, long long n, const float* avg, GridGeom g,
+                                                     fsim_particle_gfx* out, int vec) {
+    __shared__ __align__(16) float stage[GFX_THREADS * 5];
+    const long long i0 = (long long)blockIdx.x * GFX_THREADS;
+    const long long i = i0 + threadIdx.x;
+    float rec[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    if (i < n) {
+        const float px = p.p[0][i], py = p.p[1][i], pz = p.p[2][i];
+        const float vx = p.v[0][i], vy = p.v[1][i], vz = p.v[2][i];
+        const float gx = px * g.hinv - 0.5f, gy = py * g.hinv - 0.5f, gz = pz * g.hzinv - 0.5f;
+        const int bx = (int)gx, by = (int)gy, bz = (int)gz;
+        float dens = 0.f;
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-        const int x = bx + (k >> 2), y = by + ((k >> 1) & 1), z = bz + (k & 1);
-        if (x < 0 || y < 0 || z < 0 || x >= g.nx || y >= g.ny || z >= g.nz) continue;
-        const float w = (1.f - fabsf(gx - x)) * (1.f - fabsf(gy - y)) * (1.f - fabsf(gz - z));
-        dens += w * avg[gidx(g, x, y, z)];
+        for (int k = 0; k < 8; k++) {
+            const int x = bx + (k >> 2), y = by + ((k >> 1) & 1), z = bz + (k & 1);
+            if (x < 0 || y < 0 || z < 0 || x >= g.nx || y >= g.ny || z >= g.nz) continue;
+            const float w = (1.f - fabsf(gx - x)) * (1.f - fabsf(gy - y)) * (1.f - fabsf(gz - z));
+            dens += w * avg[gidx(g, x, y, z)];
+        }
+        rec[0] = px;
+        rec[1] = py;
+        rec[2] = pz;
+        rec[3] = sqrtf(vx * vx + vy * vy + vz * vz);
+        rec[4] = dens;
     }
-    fsim_particle_gfx o;
-    o.pos[0] = px; o.pos[1] = py; o.pos[2] = pz;
-    o.v = sqrtf(vx * vx + vy * vy + vz * vz);
-    o.density = dens;
-    out[i] = o;
+    if (!vec) {
+        if (i < n) {
+            fsim_particle_gfx o;
+            o.pos[0] = rec[0]; o.pos[1] = rec[1]; o.pos[2] = rec[2];
+            o.v = rec[3];
+            o.density = rec[4];
+            out[i] = o;
+        }
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < 5; k++) stage[threadIdx.x * 5 + k] = rec[k];
+    __syncthreads();
+    const long long nrec = n - i0 < GFX_THREADS ? n - i0 : GFX_THREADS;
+    const int nfl = (int)(nrec * 5), nf4 = nfl >> 2;
+    float* dst = reinterpret_cast<float*>(out) + i0 * 5;
+    for (int q = threadIdx.x; q < nf4; q += GFX_THREADS)
+        reinterpret_cast<float4*>(dst)[q] = reinterpret_cast<const float4*>(stage)[q];
+    if ((int)threadIdx.x < nfl - 4 * nf4) dst[4 * nf4 + threadIdx.x] = stage[4 * nf4 + threadIdx.x];
 }
 
 }  // namespace
@@ -516,5 +546,6 @@ void launch_spawn_disc(ParticleBuf p, long long first, int ncells, const fsim_ob
 void launch_gfx(ParticleBuf p, long long n, const float* avg, const GridGeom& g,
                 fsim_particle_gfx* out, cudaStream_t s) {
     if (n <= 0) return;
-    k_gfx<<<ceil_div(n, 256), 256, 0, s>>>(p, n, avg, g, out);
+    const int vec = (reinterpret_cast<uintptr_t>(out) & 15) == 0 ? 1 : 0;
+    k_gfx<<<ceil_div(n, GFX_THREADS), GFX_THREADS, 0, s>>>(p, n, avg, g, out, vec);
 }
