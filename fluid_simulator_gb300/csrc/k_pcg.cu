@@ -626,14 +626,22 @@ __device__ __forceinline__ float nbsum(const Q7& q, int i, uint16_t cc) {
 }
 
 // all quads of a coarse level, thread i0 + k * step
+// (x, y, z0) of quad i of a level, in 32-bit arithmetic (levels stay below 2^31 cells)
+__device__ __forceinline__ void quad_xyz(const MGLev& L, long long i, int& x, int& y, int& z0) {
+    const unsigned iu = (unsigned)i, qz = (unsigned)(L.pz >> 2), ny = (unsigned)L.ny;
+    const unsigned t = iu / qz;
+    z0 = (int)(iu - t * qz) << 2;
+    const unsigned u = t / ny;
+    y = (int)(t - u * ny);
+    x = (int)u;
+}
+
 template <typename F>
 __device__ __forceinline__ void mg_for_range(const MGLev& L, long long i0, long long step, F&& fn) {
-    const int qz = L.pz >> 2;
-    const long long n = (long long)L.nx * L.ny * qz;
+    const long long n = (long long)L.nx * L.ny * (L.pz >> 2);
     for (long long i = i0; i < n; i += step) {
-        const int z0 = (int)(i % qz) << 2;
-        const long long t = i / qz;
-        const int y = (int)(t % L.ny), x = (int)(t / L.ny);
+        int x, y, z0;
+        quad_xyz(L, i, x, y, z0);
         fn(x, y, z0, ((long long)x * L.ny + y) * L.pz + z0);
     }
 }
@@ -651,15 +659,7 @@ __device__ __forceinline__ void mg_for_quads(const PcgArgs& A, const MGLev& L, F
             fn(x, y, z0, ((long long)x * L.ny + y) * L.pz + z0);
         }
     } else {
-        const int qz = L.pz >> 2;
-        const long long n = (long long)L.nx * L.ny * qz;
-        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-             i += (long long)gridDim.x * blockDim.x) {
-            const int z0 = (int)(i % qz) << 2;
-            const long long t = i / qz;
-            const int y = (int)(t % L.ny), x = (int)(t / L.ny);
-            fn(x, y, z0, ((long long)x * L.ny + y) * L.pz + z0);
-        }
+        mg_for_range(L, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, fn);
     }
 }
 
@@ -1599,9 +1599,8 @@ __global__ void k_mg_coarsen(MGLev F, const uint8_t* fkind, const uint8_t* fflag
     const long long n = (long long)Cl.nx * Cl.ny * Cl.nz;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int cz = (int)(i % Cl.nz);
-    const long long t = i / Cl.nz;
-    const int cy = (int)(t % Cl.ny), cx = (int)(t / Cl.ny);
+    const unsigned iu = (unsigned)i, t = iu / (unsigned)Cl.nz, u = t / (unsigned)Cl.ny;
+    const int cz = (int)(iu - t * (unsigned)Cl.nz), cy = (int)(t - u * (unsigned)Cl.ny), cx = (int)u;
     const long long ci = ((long long)cx * Cl.ny + cy) * Cl.pz + cz;
     int best = 2;
     for (int o = 0; o < 8; o++) {
@@ -1621,9 +1620,8 @@ __global__ void k_mg_code(MGLev L, const uint8_t* kind, uint16_t* code) {
     const long long n = (long long)L.nx * L.ny * L.nz;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int z = (int)(i % L.nz);
-    const long long t = i / L.nz;
-    const int y = (int)(t % L.ny), x = (int)(t / L.ny);
+    const unsigned iu = (unsigned)i, t = iu / (unsigned)L.nz, u = t / (unsigned)L.ny;
+    const int z = (int)(iu - t * (unsigned)L.nz), y = (int)(t - u * (unsigned)L.ny), x = (int)u;
     const long long ci = ((long long)x * L.ny + y) * L.pz + z;
     if (kind[ci] != 0) {
         code[ci] = 0;
