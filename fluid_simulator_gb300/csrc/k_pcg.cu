@@ -209,8 +209,10 @@ __global__ void k_setup(const SetupArgs a) {
 }
 
 // ordered compaction of active bricks (one CTA)
-__global__ void __launch_bounds__(1024) k_compact_bricks(const uint8_t* flag, long long nb, int* list,
-                                                         int* count) {
+// also the brick coordinates of each list entry (int4 {bx, by, bz, b}), so the
+// quad kernels take them with one load instead of three integer divisions
+__global__ void __launch_bounds__(1024) k_compact_bricks(const uint8_t* flag, long long nb, int nby, int nbz,
+                                                         int* list, int4* xyz, int* count) {
     __shared__ int warp_tot[32];
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
@@ -224,7 +226,12 @@ __global__ void __launch_bounds__(1024) k_compact_bricks(const uint8_t* flag, lo
         __syncthreads();
         int before = 0;
         for (int w = 0; w < warp; w++) before += warp_tot[w];
-        if (f) list[carry + before + __popc(bal & ((1u << lane) - 1u))] = (int)j;
+        if (f) {
+            const int pos = carry + before + __popc(bal & ((1u << lane) - 1u));
+            const unsigned ju = (unsigned)j, t = ju / (unsigned)nbz, u = t / (unsigned)nby;
+            list[pos] = (int)j;
+            xyz[pos] = make_int4((int)u, (int)(t - u * (unsigned)nby), (int)(ju - t * (unsigned)nbz), (int)j);
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
             int t = 0;
@@ -239,6 +246,7 @@ __global__ void __launch_bounds__(1024) k_compact_bricks(const uint8_t* flag, lo
 struct PcgArgs {
     BrickGeo B;
     const int* list;
+    const int4* bxyz;  // {bx, by, bz, b} of each list entry
     const int* nactive;
     const uint16_t* code;
     const double* b;
@@ -652,9 +660,8 @@ __device__ __forceinline__ void mg_for_quads(const PcgArgs& A, const MGLev& L, F
         const int nact = *A.nactive;
         const int sub = threadIdx.x >> 6, q = threadIdx.x & 63;
         for (int bk = blockIdx.x * 4 + sub; bk < nact; bk += gridDim.x * 4) {
-            const int b = A.list[bk];
-            const int bz = b % A.B.nbz, by = (b / A.B.nbz) % A.B.nby, bx = b / (A.B.nbz * A.B.nby);
-            const int x = bx * BRX + (q >> 5), y = by * BRY + ((q >> 3) & 3), z0 = bz * BRZ + ((q & 7) << 2);
+            const int4 bb = A.bxyz[bk];
+            const int x = bb.x * BRX + (q >> 5), y = bb.y * BRY + ((q >> 3) & 3), z0 = bb.z * BRZ + ((q & 7) << 2);
             if (x >= L.nx || y >= L.ny || z0 >= L.nz) continue;
             fn(x, y, z0, ((long long)x * L.ny + y) * L.pz + z0);
         }
@@ -1670,6 +1677,7 @@ int solver_alloc(fsim_ctx* ctx) {
     S.nbricks = (long long)S.nbx * S.nby * S.nbz;
     const size_t nc = (size_t)g.ncell;
     FSIM_CUDA_TRY(ctx, cudaMalloc(&S.brick_list, S.nbricks * sizeof(int)));
+    FSIM_CUDA_TRY(ctx, cudaMalloc(&S.brick_xyz, S.nbricks * sizeof(int4)));
     FSIM_CUDA_TRY(ctx, cudaMalloc(&S.d_nactive, sizeof(int)));
     FSIM_CUDA_TRY(ctx, cudaMalloc(&S.brick_flag, S.nbricks));
     FSIM_CUDA_TRY(ctx, cudaMalloc(&S.code, nc * sizeof(uint16_t)));
@@ -1905,7 +1913,7 @@ static int alloc_fp64(fsim_ctx* ctx) {
 
 void solver_free(fsim_ctx* ctx) {
     SolverBufs& S = ctx->sv;
-    cudaFree(S.brick_list); cudaFree(S.d_nactive); cudaFree(S.brick_flag); cudaFree(S.code);
+    cudaFree(S.brick_list); cudaFree(S.brick_xyz); cudaFree(S.d_nactive); cudaFree(S.brick_flag); cudaFree(S.code);
     cudaFree(S.b); cudaFree(S.phi); cudaFree(S.r); cudaFree(S.r64); cudaFree(S.partials);
     cudaFree(S.counter); cudaFree(S.st); cudaFreeHost(S.st_host); cudaFree(S.guess);
     if (S.iter_exec) cudaGraphExecDestroy(S.iter_exec);
@@ -2158,7 +2166,8 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     sa.phi = S.phi;
     sa.brick_flag = S.brick_flag;
     k_setup<<<ceil_div(g.ncell, 256), 256, 0, st>>>(sa);
-    k_compact_bricks<<<1, 1024, 0, st>>>(S.brick_flag, S.nbricks, S.brick_list, S.d_nactive);
+    k_compact_bricks<<<1, 1024, 0, st>>>(S.brick_flag, S.nbricks, S.nby, S.nbz, S.brick_list, S.brick_xyz,
+                                         S.d_nactive);
     ctx->launches += 2;
     fetch_small(&ctx->h_misc[1], S.d_nactive, (int)sizeof(int), st);
 
@@ -2177,6 +2186,7 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     PcgArgs A;
     A.B = B;
     A.list = S.brick_list;
+    A.bxyz = S.brick_xyz;
     A.nactive = S.d_nactive;
     A.code = S.code;
     A.b = S.b;
