@@ -49,8 +49,7 @@ struct SolverBufs {
     double conv_rate = 0.0;    // measured PCG residual-norm factor per iteration (chunk planning)
     int nbx, nby, nbz;         // bricks per axis
     long long nbricks;
-    int* brick_list = nullptr; // active bricks (contain a fluid cell), ascending
-    int4* brick_xyz = nullptr; // their brick coordinates {bx, by, bz, b}
+    int4* brick_xyz = nullptr; // active bricks (contain a fluid cell), ascending: {bx, by, bz, b}
     int* d_nactive = nullptr;  // device count of active bricks
     uint8_t* brick_flag = nullptr;
     uint16_t* code = nullptr;  // per cell: fluid-neighbour mask, non-solid count, self fluid

@@ -92,12 +92,12 @@ __device__ __forceinline__ long long nb_off(const BrickGeo& B, int k) {
     return (k & 1) ? -st : st;
 }
 
-__device__ __forceinline__ bool brick_cell(const BrickGeo& B, int b, int t, int& x, int& y, int& z,
+// cell t of active brick bb = {bx, by, bz, b} (the compacted list's coordinates)
+__device__ __forceinline__ bool brick_cell(const BrickGeo& B, int4 bb, int t, int& x, int& y, int& z,
                                            long long& c) {
-    const int bz = b % B.nbz, by = (b / B.nbz) % B.nby, bx = b / (B.nbz * B.nby);
-    x = bx * BRX + t / (BRY * BRZ);
-    y = by * BRY + (t / BRZ) % BRY;
-    z = bz * BRZ + t % BRZ;
+    x = bb.x * BRX + t / (BRY * BRZ);
+    y = bb.y * BRY + (t / BRZ) % BRY;
+    z = bb.z * BRZ + t % BRZ;
     if (x >= B.g.nx || y >= B.g.ny || z >= B.g.nz) return false;
     c = gidx(B.g, x, y, z);
     return true;
@@ -209,10 +209,10 @@ __global__ void k_setup(const SetupArgs a) {
 }
 
 // ordered compaction of active bricks (one CTA)
-// also the brick coordinates of each list entry (int4 {bx, by, bz, b}), so the
-// quad kernels take them with one load instead of three integer divisions
+// each entry holds the brick's coordinates and index, int4 {bx, by, bz, b}, so
+// the kernels over active bricks take them with one load, not three divisions
 __global__ void __launch_bounds__(1024) k_compact_bricks(const uint8_t* flag, long long nb, int nby, int nbz,
-                                                         int* list, int4* xyz, int* count) {
+                                                         int4* xyz, int* count) {
     __shared__ int warp_tot[32];
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
@@ -229,7 +229,6 @@ __global__ void __launch_bounds__(1024) k_compact_bricks(const uint8_t* flag, lo
         if (f) {
             const int pos = carry + before + __popc(bal & ((1u << lane) - 1u));
             const unsigned ju = (unsigned)j, t = ju / (unsigned)nbz, u = t / (unsigned)nby;
-            list[pos] = (int)j;
             xyz[pos] = make_int4((int)u, (int)(t - u * (unsigned)nby), (int)(ju - t * (unsigned)nbz), (int)j);
         }
         __syncthreads();
@@ -245,8 +244,7 @@ __global__ void __launch_bounds__(1024) k_compact_bricks(const uint8_t* flag, lo
 
 struct PcgArgs {
     BrickGeo B;
-    const int* list;
-    const int4* bxyz;  // {bx, by, bz, b} of each list entry
+    const int4* bxyz;  // active bricks, ascending: {bx, by, bz, b}
     const int* nactive;
     const uint16_t* code;
     const double* b;
@@ -280,7 +278,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_residual(const PcgArgs a, Vecs<
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int x, y, z;
         long long c;
-        if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, z, c)) continue;
+        if (!brick_cell(a.B, a.bxyz[bk], threadIdx.x, x, y, z, c)) continue;
         const uint16_t cc = a.code[c];
         if (!(cc & CODE_FLUID)) continue;
         const double* phi = a.phi;
@@ -335,7 +333,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_black(const PcgArgs a, Vecs<T> 
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int x, y, z;
         long long c;
-        if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, z, c)) continue;
+        if (!brick_cell(a.B, a.bxyz[bk], threadIdx.x, x, y, z, c)) continue;
         if (((x + y + z) & 1) == 0) continue;
         const uint16_t cc = a.code[c];
         if (!(cc & CODE_FLUID)) continue;
@@ -365,7 +363,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_red(const PcgArgs a, Vecs<T> v,
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int x, y, z;
         long long c;
-        if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, z, c)) continue;
+        if (!brick_cell(a.B, a.bxyz[bk], threadIdx.x, x, y, z, c)) continue;
         const uint16_t cc = a.code[c];
         if (!(cc & CODE_FLUID)) continue;
         const T rv = r[c];
@@ -423,7 +421,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_spmv(const PcgArgs a, Vecs<T> v
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int x, y, z;
         long long c;
-        if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, z, c)) continue;
+        if (!brick_cell(a.B, a.bxyz[bk], threadIdx.x, x, y, z, c)) continue;
         const uint16_t cc = a.code[c];
         if (!(cc & CODE_FLUID)) continue;
         // beta = 0 (first iteration, after a restart): s = z exactly, without
@@ -473,7 +471,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int x, y, z;
         long long c;
-        if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, z, c)) continue;
+        if (!brick_cell(a.B, a.bxyz[bk], threadIdx.x, x, y, z, c)) continue;
         const uint16_t cc = a.code[c];
         if (!(cc & CODE_FLUID)) continue;
         v.x[c] += alpha * s[c];
@@ -1655,7 +1653,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_fold(const PcgArgs a, float* x)
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int xx, y, z;
         long long c;
-        if (!brick_cell(a.B, a.list[bk], threadIdx.x, xx, y, z, c)) continue;
+        if (!brick_cell(a.B, a.bxyz[bk], threadIdx.x, xx, y, z, c)) continue;
         if (!(a.code[c] & CODE_FLUID)) continue;
         a.phi[c] += (double)x[c];
         x[c] = 0.f;
@@ -1676,7 +1674,6 @@ int solver_alloc(fsim_ctx* ctx) {
     S.nbz = ceil_div(g.nz, BRZ);
     S.nbricks = (long long)S.nbx * S.nby * S.nbz;
     const size_t nc = (size_t)g.ncell;
-    FSIM_CUDA_TRY(ctx, cudaMalloc(&S.brick_list, S.nbricks * sizeof(int)));
     FSIM_CUDA_TRY(ctx, cudaMalloc(&S.brick_xyz, S.nbricks * sizeof(int4)));
     FSIM_CUDA_TRY(ctx, cudaMalloc(&S.d_nactive, sizeof(int)));
     FSIM_CUDA_TRY(ctx, cudaMalloc(&S.brick_flag, S.nbricks));
@@ -1913,7 +1910,7 @@ static int alloc_fp64(fsim_ctx* ctx) {
 
 void solver_free(fsim_ctx* ctx) {
     SolverBufs& S = ctx->sv;
-    cudaFree(S.brick_list); cudaFree(S.brick_xyz); cudaFree(S.d_nactive); cudaFree(S.brick_flag); cudaFree(S.code);
+    cudaFree(S.brick_xyz); cudaFree(S.d_nactive); cudaFree(S.brick_flag); cudaFree(S.code);
     cudaFree(S.b); cudaFree(S.phi); cudaFree(S.r); cudaFree(S.r64); cudaFree(S.partials);
     cudaFree(S.counter); cudaFree(S.st); cudaFreeHost(S.st_host); cudaFree(S.guess);
     if (S.iter_exec) cudaGraphExecDestroy(S.iter_exec);
@@ -1936,7 +1933,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_guess_judge(const PcgArgs a, co
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int x, y, z;
         long long c;
-        if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, z, c)) continue;
+        if (!brick_cell(a.B, a.bxyz[bk], threadIdx.x, x, y, z, c)) continue;
         const uint16_t cc = a.code[c];
         if (!(cc & CODE_FLUID)) continue;
         const float ns = (float)code_ns(cc);
@@ -1964,7 +1961,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_guess_apply(const PcgArgs a, co
     for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
         int x, y, z;
         long long c;
-        if (!brick_cell(a.B, a.list[bk], threadIdx.x, x, y, z, c)) continue;
+        if (!brick_cell(a.B, a.bxyz[bk], threadIdx.x, x, y, z, c)) continue;
         if (a.code[c] & CODE_FLUID) a.phi[c] = (double)guess[c];
     }
 }
@@ -2166,8 +2163,7 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     sa.phi = S.phi;
     sa.brick_flag = S.brick_flag;
     k_setup<<<ceil_div(g.ncell, 256), 256, 0, st>>>(sa);
-    k_compact_bricks<<<1, 1024, 0, st>>>(S.brick_flag, S.nbricks, S.nby, S.nbz, S.brick_list, S.brick_xyz,
-                                         S.d_nactive);
+    k_compact_bricks<<<1, 1024, 0, st>>>(S.brick_flag, S.nbricks, S.nby, S.nbz, S.brick_xyz, S.d_nactive);
     ctx->launches += 2;
     fetch_small(&ctx->h_misc[1], S.d_nactive, (int)sizeof(int), st);
 
@@ -2185,7 +2181,6 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
 
     PcgArgs A;
     A.B = B;
-    A.list = S.brick_list;
     A.bxyz = S.brick_xyz;
     A.nactive = S.d_nactive;
     A.code = S.code;
