@@ -526,11 +526,12 @@ __global__ void __launch_bounds__(PCG_THREADS) k_update(const PcgArgs a, Vecs<T>
 // 4 R (f - L x) with R the full-weighting restriction (R = P^T / 8, P the
 // cell-centred trilinear prolongation, weights 3/4 and 1/4 per axis).  The
 // smoother is red-black Gauss-Seidel, NU sweeps red->black before the coarse
-// correction and black->red after it; the coarsest level (<= 512 cells) is
-// smoothed BOTTOM times each way inside one CTA.  Starting every level from
-// zero, the V-cycle is a fixed symmetric linear operator, as CG requires.
-// Sweeps per level group, measured on the 256^3 fill workload (PCG to 1e-6,
-// steps/s of the whole step): (2, 2, 2) took 30 iterations; (3, 6, 6) 16.3
+// correction and black->red after it; the coarsest level (at most 4 cells per
+// axis) is smoothed BOTTOM times each way inside one CTA.  Starting every level
+// from zero, the V-cycle is a fixed symmetric linear operator, as CG requires.
+// Sweeps per level group, first measured on the 256^3 fill workload (PCG to 1e-6,
+// steps/s of the whole step; the defaults below were re-measured after the
+// coarse levels got cheaper): (2, 2, 2) took 30 iterations; (3, 6, 6) 16.3
 // iterations, 34.0 steps/s; (2, 6, 6) 17 iterations, 35.4; (1, 6, 6) 18.8, 35.8;
 // (2, 4, 6) 17.8, 35.3.  A fine-level sweep costs ~107 us in place, a level-1
 // sweep ~22 us: the coarse correction near the free surface is the weak part of
