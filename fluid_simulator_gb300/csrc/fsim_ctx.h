@@ -180,8 +180,9 @@ void launch_gfx(ParticleBuf p, long long n, const float* avg, const GridGeom& g,
 void launch_p2g(fsim_ctx* ctx);
 int launch_g2p(fsim_ctx* ctx);
 bool make_tensor_maps(fsim_ctx* ctx);
-void launch_p2g_raw(ParticleBuf p, const uint32_t* perm, const int* cstart, const GridGeom& g, float* const u[3],
-                    uint8_t* flags, float* avg, bool apic, cudaStream_t stream);
+// Returns the launch's error (a failed shared-memory attribute set included).
+cudaError_t launch_p2g_raw(ParticleBuf p, const uint32_t* perm, const int* cstart, const GridGeom& g,
+                           float* const u[3], uint8_t* flags, float* avg, bool apic, cudaStream_t stream);
 
 // ---- launchers (k_grid.cu) -------------------------------------------------
 int launch_obstacle(fsim_ctx* ctx, const fsim_obstacle& o);  // returns kernels launched

@@ -16,7 +16,12 @@
 // library's kernels are loaded holds its FSIM_NOALLOC_SCRATCH_BYTES until the
 // process exits.  Host code cannot use the array's name as a device address;
 // the first call on each device (with that device current) looks the address
-// up with cudaGetSymbolAddress and caches it.
+// up with cudaGetSymbolAddress and caches it.  With CUDA's default lazy module
+// loading that lookup is also where the library's module is loaded on the
+// device and the array reserved -- an implicit device allocation that can
+// synchronise the device -- so callers make their first call at set-up time
+// (or run with CUDA_MODULE_LOADING=EAGER).
+#include <cmath>
 #include <mutex>
 
 #include "fsim_ctx.h"
@@ -68,7 +73,7 @@ extern "C" int fsim_p2g_noalloc(const fsim_grid_desc* grid, int transfer, const 
                                 float* avg, void* stream) {
     if (!grid || !pos || !vel || !vx || !vy || !vz || !flags || !avg || n < 0) return FSIM_E_INVALID;
     if (transfer < FSIM_PIC || transfer > FSIM_APIC || (transfer == FSIM_APIC && !c)) return FSIM_E_INVALID;
-    if (grid->two_d || !(grid->resolution > 0)) return FSIM_E_INVALID;
+    if (grid->two_d || !(grid->resolution > 0) || !std::isfinite(grid->resolution)) return FSIM_E_INVALID;
     // grid geometry as fsim_create derives it (MacGrid ctor, macGrid.cpp:9-13)
     GridGeom g{};
     g.hd = 1 / (double)(float)grid->resolution;
@@ -79,15 +84,28 @@ extern "C" int fsim_p2g_noalloc(const fsim_grid_desc* grid, int transfer, const 
     g.hzinvd = g.hinvd;
     g.hz = g.h;
     g.hzinv = g.hinv;
-    g.nx = (int)(grid->dims[0] / g.hd);
-    g.ny = (int)(grid->dims[1] / g.hd);
-    g.nz = (int)(grid->dims[2] / g.hd);
+    // cells per axis, bounded in floating point before any integer conversion
+    // (a product of three in-range axes can still wrap a 64-bit count)
+    double cells_axis[3];
+    for (int a = 0; a < 3; a++) {
+        if (!std::isfinite(grid->dims[a]) || !(grid->dims[a] > 0)) return FSIM_E_INVALID;
+        cells_axis[a] = std::floor(grid->dims[a] / g.hd);
+        if (!(cells_axis[a] <= (double)kMaxCells)) return FSIM_E_CAPACITY;
+    }
+    if (!(cells_axis[0] * cells_axis[1] * cells_axis[2] <= (double)kMaxCells)) return FSIM_E_CAPACITY;
+    g.nx = (int)cells_axis[0];
+    g.ny = (int)cells_axis[1];
+    g.nz = (int)cells_axis[2];
     if (g.nx < 3 || g.ny < 3 || g.nz < 3) return FSIM_E_INVALID;
     if (g.nz % 4 != 0) return FSIM_E_INVALID;  // outputs are dense: z rows must need no padding
     g.pz = g.nz;
     g.ncell = (long long)g.nx * g.ny * g.nz;
     for (int a = 0; a < 3; a++) g.dims[a] = (a == 0 ? g.nx : a == 1 ? g.ny : g.nz) * g.hd;
     if ((size_t)n > kMaxParticles || (size_t)g.ncell > kMaxCells) return FSIM_E_CAPACITY;
+    // an error left pending by the caller's earlier work on this thread is
+    // reported before anything is launched (and left pending), so that the
+    // final launch check below reports only this call's launches
+    if (cudaPeekAtLastError() != cudaSuccess) return FSIM_E_CUDA;
 
     unsigned char* base = nullptr;
     if (scratch_address(&base) != cudaSuccess) return FSIM_E_CUDA;
@@ -123,6 +141,7 @@ extern "C" int fsim_p2g_noalloc(const fsim_grid_desc* grid, int transfer, const 
     launch_scan(count, cstart, g.ncell, blocks, s);
     launch_scatter(key, rank, cstart, perm, n, s);
     float* const u[3] = {vx, vy, vz};
-    launch_p2g_raw(p, perm, cstart, g, u, flags, avg, transfer == FSIM_APIC, s);
+    if (launch_p2g_raw(p, perm, cstart, g, u, flags, avg, transfer == FSIM_APIC, s) != cudaSuccess)
+        return FSIM_E_CUDA;
     return cudaGetLastError() == cudaSuccess ? FSIM_OK : FSIM_E_CUDA;
 }

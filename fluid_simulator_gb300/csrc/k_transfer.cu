@@ -512,8 +512,8 @@ void launch_p2g(fsim_ctx* ctx) {
 
 // P2G on caller-provided buffers (used by the allocation-free entry point in
 // fsim_static.cu); same kernel as launch_p2g.
-void launch_p2g_raw(ParticleBuf p, const uint32_t* perm, const int* cstart, const GridGeom& g, float* const u[3],
-                    uint8_t* flags, float* avg, bool apic, cudaStream_t stream) {
+cudaError_t launch_p2g_raw(ParticleBuf p, const uint32_t* perm, const int* cstart, const GridGeom& g,
+                           float* const u[3], uint8_t* flags, float* avg, bool apic, cudaStream_t stream) {
     P2GArgs a;
     a.p = p;
     a.perm = perm;
@@ -526,12 +526,13 @@ void launch_p2g_raw(ParticleBuf p, const uint32_t* perm, const int* cstart, cons
     a.nty = ceil_div(g.ny, PY);
     a.ntz = ceil_div(g.nz, PZ);
     const int nb = a.ntx * a.nty * a.ntz;
-    set_smem_limit((const void*)k_p2g<false>, P2G_SMEM);
-    set_smem_limit((const void*)k_p2g<true>, P2G_SMEM);
+    cudaError_t e = set_smem_limit((const void*)(apic ? k_p2g<true> : k_p2g<false>), P2G_SMEM);
+    if (e != cudaSuccess) return e;
     if (apic)
         k_p2g<true><<<nb, P2G_THREADS, P2G_SMEM, stream>>>(a);
     else
         k_p2g<false><<<nb, P2G_THREADS, P2G_SMEM, stream>>>(a);
+    return cudaGetLastError();
 }
 
 // TMA descriptors of the six face arrays (v2 x/y/z, v x/y/z): 3D tensors

@@ -339,12 +339,26 @@ int fsim_solve_current(fsim_ctx *ctx, double dt, int warm_start, int apply, fsim
  * part that must start at zero), so calls whose work overlaps on the GPU --
  * on different streams, or from different host threads -- race and must not
  * be issued.  The first call on a device, made with that device current,
- * looks up the array's device address (cudaGetSymbolAddress); make that first
- * call before capturing any stream.
+ * looks up the array's device address (cudaGetSymbolAddress).  Under CUDA's
+ * default lazy module loading, that first call is also where the library's
+ * module is loaded on the device and the array reserved, which is a device
+ * allocation in effect and can synchronise the device: make the first call at
+ * set-up time, before any frame-budgeted work and before capturing any stream
+ * (or set CUDA_MODULE_LOADING=EAGER, which reserves it when the library's
+ * module loads).
  *
  * Limits.  n <= FSIM_NOALLOC_MAX_PARTICLES and nx*ny*nz <=
- * FSIM_NOALLOC_MAX_CELLS, else FSIM_E_CAPACITY; nz must be a multiple of 4
- * (FSIM_E_INVALID otherwise).  Grid geometry follows fsim_grid_desc.
+ * FSIM_NOALLOC_MAX_CELLS (each axis checked before the product), else
+ * FSIM_E_CAPACITY; non-finite or non-positive dims or resolution, or nz not a
+ * multiple of 4, give FSIM_E_INVALID.  Grid geometry follows fsim_grid_desc.
+ * Positions must lie inside the grid, [0, dims) on every axis, as the
+ * context path's advection leaves them; a particle outside is counted in the
+ * nearest edge cell, and its weights there have no meaning.
+ *
+ * Errors.  A CUDA error already pending on the calling thread when the call
+ * starts is returned as FSIM_E_CUDA before anything is launched, and left
+ * pending for the caller; after that, FSIM_E_CUDA reports this call's own
+ * launch failures.
  *
  * Buffers (all device memory, stream-ordered on `stream`, a cudaStream_t or
  * NULL for the default stream): pos and vel hold 3 planes of n floats

@@ -21,8 +21,10 @@
 // valid until the next simulate().
 //
 // Parts of the reference interface that only the reference's own Simulator
-// uses internally (face/cell stencil helpers, grid reset, P2G helpers, the
-// intersection hash) are not declared.  Push-apart runs with the library's
+// uses internally (grid reset, P2G helpers, the intersection hash) are not
+// declared; the stencil accessors getFacesAround / getCellsAround and the
+// trilinear helpers of util/interpolation.h are, since callers of the
+// Simulator (the manager's gfx fill) use them.  Push-apart runs with the library's
 // deterministic (Jacobi) semantics.  BasicMacGrid selects the library's SOR
 // solver.  Default particle positions of HashedParticles
 // use a SplitMix64 generator instead of std::rand.
@@ -41,6 +43,7 @@
 #include <string>
 #include <utility>
 #include <vector>
+#include <array>
 #include <atomic>
 
 #include "fsim.h"
@@ -370,6 +373,47 @@ public:
 
     MacGridCell& getCellAt(const glm::dvec3& p) { return cell(glm::ivec3(p * cellDInv)); }
 
+    // Reference: macGrid.h:40 / macGrid.cpp:142-181.  The 8 faces of each axis
+    // whose trilinear weights at `p` can be non-zero: for axis a the position in
+    // cell units is shifted by half a cell on the two other axes, truncated
+    // toward zero, and moved one cell down along a (face a of cell i sits at
+    // (i + 1) h).  Entries come in the reference's corner order
+    // (+x+y+z, +y+z, +x+z, +x+y, +x, +z, +y, base); the faces are those of the
+    // host mirror (downloaded on first access after a step).
+    std::array<std::array<MacGridCell::FaceRef, 8>, 3> getFacesAround(const glm::dvec3& p) {
+        const glm::dvec3 g = p * cellDInv;
+        glm::ivec3 base[3];
+        for (int a = 0; a < 3; a++) {
+            const double s[3] = {a == 0 ? 0.0 : 0.5, a == 1 ? 0.0 : 0.5, a == 2 ? 0.0 : 0.5};
+            base[a] = glm::ivec3((int)(g.x - s[0]), (int)(g.y - s[1]), (int)(g.z - s[2]));
+            base[a][a] -= 1;
+        }
+        auto face = [&](int a, int k) -> MacGridCell::FaceRef {
+            const glm::ivec3 o = corner(k);
+            return MacGridCell::FaceRef{cell(base[a].x + o.x, base[a].y + o.y, base[a].z + o.z).faces[a]};
+        };
+        return {std::array<MacGridCell::FaceRef, 8>{face(0, 0), face(0, 1), face(0, 2), face(0, 3), face(0, 4),
+                                                    face(0, 5), face(0, 6), face(0, 7)},
+                std::array<MacGridCell::FaceRef, 8>{face(1, 0), face(1, 1), face(1, 2), face(1, 3), face(1, 4),
+                                                    face(1, 5), face(1, 6), face(1, 7)},
+                std::array<MacGridCell::FaceRef, 8>{face(2, 0), face(2, 1), face(2, 2), face(2, 3), face(2, 4),
+                                                    face(2, 5), face(2, 6), face(2, 7)}};
+    }
+
+    // Reference: macGrid.h:56 / macGrid.cpp:188-202.  The 8 cells whose centres
+    // surround `p` (position in cell units minus one half, truncated toward
+    // zero), in the same corner order as getFacesAround.  The manager's gfx fill
+    // reads avgPNum through it (simulationManager.cpp:226-228).
+    std::array<MacGridCellRef, 8> getCellsAround(const glm::dvec3& p) {
+        const glm::dvec3 g = p * cellDInv;
+        const glm::ivec3 b((int)(g.x - 0.5), (int)(g.y - 0.5), (int)(g.z - 0.5));
+        auto at = [&](int k) -> MacGridCellRef {
+            const glm::ivec3 o = corner(k);
+            return MacGridCellRef{cell(b.x + o.x, b.y + o.y, b.z + o.z)};
+        };
+        return {at(0), at(1), at(2), at(3), at(4), at(5), at(6), at(7)};
+    }
+
     template <int axis = 0, int offset = 0>
     MacGridCell& cell(const glm::ivec3& p) {
         pull();
@@ -434,6 +478,13 @@ public:
 
 protected:
     friend class simulator::Simulator;
+
+    // Offset of corner k of a stencil in the reference's order.
+    static glm::ivec3 corner(int k) {
+        static const int o[8][3] = {{1, 1, 1}, {0, 1, 1}, {1, 0, 1}, {1, 1, 0},
+                                    {1, 0, 0}, {0, 0, 1}, {0, 1, 0}, {0, 0, 0}};
+        return glm::ivec3(o[k][0], o[k][1], o[k][2]);
+    }
 
     void pull() {
         if (!device || host_valid) return;
@@ -706,3 +757,21 @@ private:
 
 }  // namespace simulator
 }  // namespace genericfsim
+
+// Reference: util/interpolation.h:7-35 (global namespace, as the reference
+// declares them).  Trilinear tent weight of a node at `center` seen from `pos`,
+// prod over axes of (1 - |d|) with d the offset in cell units, and its gradient
+// with respect to `pos` (component a: -sign(d_a) times the other two factors,
+// in 1 / length units; +1 where d_a = 0).
+inline double trilinearInterpoll(const glm::dvec3& center, const glm::dvec3& pos, const glm::dvec3 invCellD) {
+    const glm::dvec3 d = (pos - center) * invCellD;
+    return (1.0 - std::fabs(d.x)) * (1.0 - std::fabs(d.y)) * (1.0 - std::fabs(d.z));
+}
+
+inline glm::dvec3 trilinearInterpollGradient(const glm::dvec3& center, const glm::dvec3& pos,
+                                             const glm::dvec3 invCellD) {
+    const glm::dvec3 d = (pos - center) * invCellD;
+    const double wx = 1.0 - std::fabs(d.x), wy = 1.0 - std::fabs(d.y), wz = 1.0 - std::fabs(d.z);
+    const double sx = d.x > 0.0 ? -1.0 : 1.0, sy = d.y > 0.0 ? -1.0 : 1.0, sz = d.z > 0.0 ? -1.0 : 1.0;
+    return glm::dvec3(sx * wy * wz, sy * wx * wz, sz * wx * wy) * invCellD;
+}

@@ -83,9 +83,21 @@ def build_port(quiet: bool = True) -> str:
     return PORT_LIB
 
 
-def build_ref(ref_dir: str = "/root/reference", quiet: bool = True) -> str | None:
+def reference_dir() -> str | None:
+    """The reference checkout (dkiovics/fluid_simulator): $FSIM_REFERENCE_DIR,
+    else the directory ``reference`` beside this repository; None when neither
+    holds the Simulator sources (e.g. on a machine that only runs the GPU tests)."""
+    cands = [os.environ.get("FSIM_REFERENCE_DIR"), os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for d in cands:
+        if d and os.path.isdir(os.path.join(d, "src", "Simulator")):
+            return d
+    return None
+
+
+def build_ref(ref_dir: str | None = None, quiet: bool = True) -> str | None:
     """Compile oracle/_ref/libfsim_ref.so when the reference sources exist."""
-    if not os.path.isdir(os.path.join(ref_dir, "src", "Simulator")):
+    ref_dir = ref_dir or reference_dir()
+    if ref_dir is None:
         return None
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={ref_dir}"], check=True,
                    stdout=subprocess.DEVNULL if quiet else None)

@@ -11,7 +11,12 @@
 // z = 0.15), as SimulationManager does for twoD (simulationManager.cpp:17,27).
 //
 // out.bin: int64 n, then pos (n x 3), v (n x 3), c (n x 9) as float32, then
-// int32 PCG iterations of the last step.
+// int32 PCG iterations of the last step, then the renderer's per-particle
+// density (n float32) computed as SimulationManager's gfx fill does it
+// (simulationManager.cpp:222-230: getCellsAround + trilinearInterpoll of
+// avgPNum).
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -84,6 +89,35 @@ int main(int argc, char** argv) {
                 for (int b = 0; b < 3; b++) c9[9 * i + 3 * a + b] = (float)q.c[a][b];
             }
         }
+        // ParticleGfxData::density, as the manager's gfx fill computes it
+        std::vector<float> dens((size_t)m);
+        parts->forEach(true, [&](particles::Particle& q, int index) {
+            float density = 0;
+            auto cells = grid->getCellsAround(q.pos);
+            for (auto& c : cells) density += trilinearInterpoll(q.pos, c.cell.pos, grid->cellDInv) * c.cell.avgPNum;
+            dens[(size_t)index] = density;
+        });
+        // the stencils are partitions of unity: for every particle the tent
+        // weights of the 8 faces of each axis (getFacesAround) and of the 8 cell
+        // centres (getCellsAround) are non-negative and sum to 1
+        for (int i = 0; i < m && !two_d; i++) {
+            const glm::dvec3 q = parts->getParticleAt(i).pos;
+            const auto faces = grid->getFacesAround(q);
+            const auto cells = grid->getCellsAround(q);
+            for (int a = 0; a < 4; a++) {
+                double sum = 0, lo = 1;
+                for (int k = 0; k < 8; k++) {
+                    const glm::dvec3 node = a < 3 ? faces[a][k].face.pos : cells[k].cell.pos;
+                    const double w = trilinearInterpoll(node, q, grid->cellDInv);
+                    sum += w;
+                    lo = std::min(lo, w);
+                }
+                if (std::fabs(sum - 1.0) > 1e-9 || lo < -1e-9) {
+                    std::cerr << "stencil " << a << " of particle " << i << ": weight sum " << sum << "\n";
+                    return 3;
+                }
+            }
+        }
         // a cell read through the grid mirror, as SimulationManager::getCellAt does
         const macgrid::MacGridCell& cell = grid->getCellAt(glm::dvec3(0.3, 0.1, zc));
         std::ofstream out(argv[6], std::ios::binary);
@@ -93,6 +127,7 @@ int main(int argc, char** argv) {
         out.write(reinterpret_cast<const char*>(v3.data()), v3.size() * 4);
         out.write(reinterpret_cast<const char*>(c9.data()), c9.size() * 4);
         out.write(reinterpret_cast<const char*>(&its), 4);
+        out.write(reinterpret_cast<const char*>(dens.data()), dens.size() * 4);
         std::cout << "particles " << m << " its " << its << " cell_type " << (int)cell.type << "\n";
     } catch (const std::exception& e) {
         std::cerr << "error: " << e.what() << "\n";

@@ -62,3 +62,30 @@ def test_struct_sizes_match_header(tmp_path):
             native.RenderParams.background.offset]
     assert got == want
 
+
+
+def test_noalloc_rejects_wrapping_grid_sizes_before_any_cuda_call(lib):
+    """fsim_p2g_noalloc bounds each axis before forming the cell count: dims whose
+    product of cells would wrap a 64-bit count are a capacity error, and
+    non-finite dims are invalid.  Both are decided before any CUDA call, so this
+    runs without a GPU."""
+    f = lib.fsim_p2g_noalloc
+    f.restype = C.c_int
+    f.argtypes = [C.POINTER(native.GridDesc), C.c_int] + [C.c_void_p] * 3 + [C.c_int64] + [C.c_void_p] * 6
+    dummy = C.c_void_p(16)  # never dereferenced
+    g = native.GridDesc()
+    g.two_d = 0
+    g.resolution = 1.0
+    g.dims[:] = [float(1 << 22), float(1 << 21), float(1 << 21)]  # 2^64 cells: wraps to 0 in 64-bit integers
+    rc = f(C.byref(g), native.FLIP, dummy, dummy, None, 10, dummy, dummy, dummy, dummy, dummy, None)
+    assert native.ERRORS[rc] == "CAPACITY"
+    g.dims[:] = [1e300, 1.0, 1.0]
+    rc = f(C.byref(g), native.FLIP, dummy, dummy, None, 10, dummy, dummy, dummy, dummy, dummy, None)
+    assert native.ERRORS[rc] == "CAPACITY"
+    g.dims[:] = [float("nan"), 1.0, 1.0]
+    rc = f(C.byref(g), native.FLIP, dummy, dummy, None, 10, dummy, dummy, dummy, dummy, dummy, None)
+    assert native.ERRORS[rc] == "INVALID"
+    g.dims[:] = [1.0, 1.0, 1.0]
+    g.resolution = float("inf")
+    rc = f(C.byref(g), native.FLIP, dummy, dummy, None, 10, dummy, dummy, dummy, dummy, dummy, None)
+    assert native.ERRORS[rc] == "INVALID"

@@ -20,6 +20,35 @@ INC = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(ROOT, "fluid_simulator_gb300")
 
 
+def test_reference_manager_compiles_against_facade(tmp_path):
+    """The reference's own SimulationManager (src/Simulator/manager), byte for
+    byte, compiles against the facade: its two files are placed unmodified in a
+    scratch tree whose simulator headers (simulator.h, basicMacGrid.h,
+    bridsonSolverGrid.h, hashedParticles.h -- the four simulationManager.h
+    includes -- and util/interpolation.h, which the .cpp includes) each forward
+    to include/fsim_facade.hpp.  Needs the reference checkout (CPU only)."""
+    import shutil
+
+    from oracle import oracle as O
+
+    ref = O.reference_dir()
+    if ref is None:
+        pytest.skip("reference checkout not present")
+    mgr = os.path.join(ref, "src", "Simulator", "manager")
+    (tmp_path / "manager").mkdir()
+    for f in ("simulationManager.h", "simulationManager.cpp"):
+        shutil.copyfile(os.path.join(mgr, f), tmp_path / "manager" / f)
+        assert (tmp_path / "manager" / f).read_bytes() == open(os.path.join(mgr, f), "rb").read()
+    for shim in ("simulator/simulator.h", "simulator/macGrid/basicMacGrid.h", "simulator/macGrid/bridsonSolverGrid.h",
+                 "simulator/particles/hashedParticles.h", "simulator/util/interpolation.h"):
+        path = tmp_path / shim
+        path.parent.mkdir(parents=True, exist_ok=True)
+        path.write_text('#pragma once\n#include "fsim_facade.hpp"\n')
+    r = subprocess.run(["g++", "-std=c++20", "-fsyntax-only", f"-I{GLM}", f"-I{INC}",
+                        str(tmp_path / "manager" / "simulationManager.cpp")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_facade_compiles():
     r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", f"-I{GLM}",
                         f"-I{INC}", DEMO], capture_output=True, text=True)
@@ -52,7 +81,9 @@ def test_facade_matches_c_abi(gpu, tmp_path, transfer, mode):
     n = int(np.frombuffer(raw[:8], np.int64)[0])
     body = np.frombuffer(raw[8:8 + 4 * 15 * n], np.float32)
     fp, fv, fc = body[:3 * n].reshape(n, 3), body[3 * n:6 * n].reshape(n, 3), body[6 * n:].reshape(n, 9)
-    its = int(np.frombuffer(raw[8 + 4 * 15 * n:], np.int32)[0])
+    its = int(np.frombuffer(raw[8 + 4 * 15 * n:8 + 4 * 15 * n + 4], np.int32)[0])
+    fdens = np.frombuffer(raw[8 + 4 * 15 * n + 4:], np.float32)
+    assert fdens.shape == (n,)
 
     h = 1.0 / res
     p = N.default_params(transfer=transfer, resolution=res, flip_ratio=0.95, gravity=-9.81, max_iters=200,
@@ -69,6 +100,7 @@ def test_facade_matches_c_abi(gpu, tmp_path, transfer, mode):
                                       speed=((x - xp) / dt, 0.0, 0.0))])
         st = sim.step(dt)
     gp, gv, gc = sim.particles()
+    gdens = sim.gfx()[:, 4]
     sim.close()
     # Same inputs, same library: the runs agree up to the order of particles
     # inside a cell (ranks come from atomics) and the differences summation
@@ -86,3 +118,7 @@ def test_facade_matches_c_abi(gpu, tmp_path, transfer, mode):
     assert np.abs(fv - gv[idx]).max() <= 1e-2 * vs
     cs = max(np.abs(gc).max(), 1e-6)
     assert np.abs(fc - gc.reshape(-1, 9)[idx]).max() <= 5e-2 * cs
+    # the manager's host-side density (getCellsAround + trilinearInterpoll over
+    # the grid mirror) against the library's device gfx publish
+    ds = max(np.abs(gdens).max(), 1e-6)
+    assert np.abs(fdens - gdens[idx]).max() <= 1e-2 * ds

@@ -97,6 +97,10 @@ def noalloc_p2g(lib, rt, pos, vel, c, transfer, res=32):
                                   davg, None)
         assert rc == 0, N.ERRORS.get(rc, rc)
         assert rt.cudaDeviceSynchronize() == 0
+        # the caller's particle buffers are inputs only: the call leaves them as they were
+        assert np.array_equal(buf.download(dpos, (3, n), np.float32), pos.T)
+        assert np.array_equal(buf.download(dvel, (3, n), np.float32), vel.T)
+        assert np.array_equal(buf.download(dc, (9, n), np.float32), c.T)
         return {N.F_VX: buf.download(outs[0], shape, np.float32), N.F_VY: buf.download(outs[1], shape, np.float32),
                 N.F_VZ: buf.download(outs[2], shape, np.float32), N.F_FLAGS: buf.download(dflags, shape, np.uint8),
                 N.F_AVGPNUM: buf.download(davg, shape, np.float32)}
