@@ -364,10 +364,121 @@ def run_fsim(args):
     if args.render:
         line["render"] = render_study(sim, N, h, peak)
     sim.close()
+    if args.parity and rank == 0 and world == 1:
+        line["parity_drift"] = {"dam32_flip_vs_live_oracle": drift_dam32(N), "dam128_vs_oracle_fixture": drift_dam128(N)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(res, dt)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- drift curves
+DRIFT_GOLDEN = os.path.join(ROOT, "tests", "golden", "drift_dam128.npz")
+
+
+def _traj_stats(sim, N):
+    """Fluid cells, mean kinetic energy, centroid, max speed (the oracle fixture's columns)."""
+    p, v, _ = sim.particles()
+    v64 = v.astype(np.float64)
+    sp2 = (v64 * v64).sum(axis=1)
+    return np.array([float((sim.grid(N.F_FLAGS) == N.WATER).sum()), 0.5 * float(sp2.mean()),
+                     *p.astype(np.float64).mean(axis=0), float(np.sqrt(sp2.max()))]), p, v
+
+
+def _curve(a, every):
+    return [float(f"{x:.3g}") for x in np.asarray(a)[every - 1::every]]
+
+
+def drift_dam32(N, every=5):
+    """32^3 FLIP dam break (dt 1/120, 100 steps), free-running on both sides from
+    the same seeded particles: the GPU and the oracle (FP64, all host threads)."""
+    from fluid_simulator_gb300.scenes import GridSpec, dam_break
+    from oracle import oracle as O
+
+    O.build_port()
+    res, dt, steps = 32, 1.0 / 120.0, 100
+    pos = dam_break(GridSpec(res), seed=0)
+    p = N.default_params(transfer=N.FLIP, resolution=res, tol=1e-6, tol_mode=N.TOL_ABS_MAX, max_iters=200)
+    sim = N.Simulation(res, p, track_ids=True)
+    sim.set_particles(pos)
+    o = O.Oracle(O.make_params(res, transfer=O.FLIP, tol=1e-6, max_iters=200), pos.astype(np.float64), lib="port")
+    o.set_threads(os.cpu_count() or 1)
+    h = sim.h
+    rows = []
+    for _ in range(steps):
+        sim.step(dt)
+        o.step(dt)
+        gs, gp, gv = _traj_stats(sim, N)
+        op, ov, _ = o.particles()
+        ke_o = 0.5 * float((ov * ov).sum(axis=1).mean())
+        vs = max(float(np.sqrt((ov * ov).sum(axis=1)).max()), 1e-9)
+        dp = np.sqrt(((gp.astype(np.float64) - op) ** 2).sum(axis=1)) / h
+        rows.append((float(np.sqrt((dp * dp).mean())), float(dp.max()),
+                     float(np.sqrt(((gv.astype(np.float64) - ov) ** 2).sum(axis=1).mean())) / vs,
+                     abs(gs[1] - ke_o) / max(ke_o, 1e-12),
+                     int(gs[0]) - int((o.grid(O.F_FLAGS) == O.WATER).sum())))
+    sim.close()
+    o.close()
+    r = np.array(rows)
+    return {"workload": "dam32_flip (32^3, FLIP 0.95, dt 1/120, 51840 particles)", "steps": steps,
+            "sampled_every": every, "position_rms_cells": _curve(r[:, 0], every),
+            "position_max_cells": _curve(r[:, 1], every), "velocity_rms_rel": _curve(r[:, 2], every),
+            "kinetic_energy_rel": _curve(r[:, 3], every), "fluid_cells_diff": [int(x) for x in r[every - 1::every, 4]]}
+
+
+def drift_dam128(N, every=10):
+    """128^3 dam break (dt 1/240, 200 steps) in PIC, FLIP 0.95 and APIC on the GPU,
+    against the oracle's free-running trajectories in tests/golden/drift_dam128.npz
+    (single-threaded FP64 oracle = the reference's results; generated by
+    tests/golden/make_drift.py).  'fp64_threads' is the same comparison between
+    two FP64 runs of the reference algorithm that differ only in the order of
+    P2G's additions (1 vs 8 OpenMP threads): the drift rounding alone causes."""
+    from fluid_simulator_gb300.scenes import GridSpec, dam_break
+
+    if not os.path.exists(DRIFT_GOLDEN):
+        return {"unavailable": "tests/golden/drift_dam128.npz missing"}
+    gold = np.load(DRIFT_GOLDEN)
+    res, dt, steps = 128, float(gold["dt"]), int(gold["steps"])
+    sample = int(gold["sample_every"])
+    tracked = gold["tracked"]
+    pos = dam_break(GridSpec(res), seed=0)
+    h = 1.0 / res
+    out = {"workload": "dam128 (128^3, dt 1/240, 3830400 particles)", "steps": steps, "sampled_every": every,
+           "tracked_particles": int(tracked.size), "tracked_every": sample}
+
+    def compare(stats, tpos, tvel, ref):
+        rs, rp, rv = gold[f"{ref}_stats"], gold[f"{ref}_pos"], gold[f"{ref}_vel"]
+        ke = np.abs(stats[:, 1] - rs[:, 1]) / np.maximum(rs[:, 1], 1e-12)
+        cen = np.sqrt(((stats[:, 2:5] - rs[:, 2:5]) ** 2).sum(axis=1)) / h
+        cells = (stats[:, 0] - rs[:, 0]) / np.maximum(rs[:, 0], 1)
+        dpos = np.sqrt(((tpos.astype(np.float64) - rp) ** 2).sum(axis=2)) / h
+        vs = np.maximum(np.sqrt((rv.astype(np.float64) ** 2).sum(axis=2)).max(axis=1), 1e-9)
+        dvel = np.sqrt(((tvel.astype(np.float64) - rv) ** 2).sum(axis=2).mean(axis=1)) / vs
+        return {"kinetic_energy_rel": _curve(ke, every), "centroid_cells": _curve(cen, every),
+                "fluid_cells_rel": _curve(cells, every),
+                "tracked_position_rms_cells": [float(f"{x:.3g}") for x in np.sqrt((dpos ** 2).mean(axis=1))],
+                "tracked_velocity_rms_rel": [float(f"{x:.3g}") for x in dvel]}
+
+    for name, transfer in (("pic", N.PIC), ("flip", N.FLIP), ("apic", N.APIC)):
+        p = N.default_params(transfer=transfer, resolution=res, tol=1e-6, tol_mode=N.TOL_ABS_MAX, max_iters=200)
+        sim = N.Simulation(res, p, track_ids=True)
+        sim.set_particles(pos)
+        stats, tp, tv, its = [], [], [], []
+        for s in range(1, steps + 1):
+            st = sim.step(dt)
+            its.append(st.pcg_iterations)
+            row, pp, vv = _traj_stats(sim, N)
+            stats.append(row)
+            if s % sample == 0:
+                tp.append(pp[tracked])
+                tv.append(vv[tracked])
+        sim.close()
+        out[name] = compare(np.array(stats), np.array(tp), np.array(tv), name)
+        out[name]["gpu_pcg_iterations_mean"] = round(float(np.mean(its)), 2)
+        out[name]["oracle_pcg_iterations_mean"] = round(float(gold[f"{name}_stats"][:, 6].mean()), 2)
+    ref = gold["flip_threads8_stats"]
+    out["fp64_threads"] = compare(ref, gold["flip_threads8_pos"], gold["flip_threads8_vel"], "flip")
+    return out
 
 
 # ---------------------------------------------------------------- renderer
@@ -627,7 +738,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precond", default="mg", choices=["mg", "rbic"],
                     help="pressure preconditioner: multigrid V-cycle or red-black incomplete Cholesky")
-    ap.add_argument("--out-dir", default=os.path.join(ROOT, "gpurun_out"))
+    ap.add_argument("--out-dir", default=os.path.join(ROOT, "bench_out"),
+                    help="where the clock samples of the timed region are written")
     ap.add_argument("--mg-sweeps", type=int, default=0,
                     help="multigrid smoothing sweeps before and after the coarse correction (0: library default)")
     ap.add_argument("--mg-coarse-sweeps", type=int, default=0,
@@ -640,6 +752,9 @@ def main():
                     help="problems of the zero / previous / learned warm-start comparison (0: skip)")
     ap.add_argument("--ws-problems", type=int, default=48, help="synthetic training problems at 64^3")
     ap.add_argument("--render", type=int, default=1, help="time one 1000x1000 frame of the headless renderer")
+    ap.add_argument("--parity", type=int, default=1,
+                    help="free-running drift curves against the oracle: 32^3 FLIP (100 steps, oracle run live) "
+                         "and 128^3 PIC / FLIP / APIC (200 steps, oracle trajectories from tests/golden) (0: skip)")
     ap.add_argument("--refine-digits", type=int, default=0,
                     help="mixed-precision refinement every 10^k residual drop (0: library default 3)")
     ap.add_argument("--ws-iters", type=int, default=1500, help="Adam iterations of the warm-start network")

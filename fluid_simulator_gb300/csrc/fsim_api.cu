@@ -206,8 +206,8 @@ void fill_advect_args(fsim_ctx* ctx, AdvectArgs& a, double dt) {
 // counting sort by cell of the current buffer (keys from do_key)
 int sort_by_cell(fsim_ctx* ctx) {
     launch_scan(ctx->count, ctx->cstart, ctx->g.ncell, ctx->scan_blocks, ctx->stream);
-    launch_scatter(ctx->key, ctx->rank, ctx->cstart, ctx->perm, ctx->n, ctx->stream);
-    ctx->launches += 3 + (ctx->n > 0 ? 1 : 0);
+    launch_scatter(ctx->key, ctx->rank, ctx->cstart, ctx->perm, ctx->n, ctx->g.ncell, ctx->stream);
+    ctx->launches += 3 + (ctx->n > 0 ? 2 : 0);
     fetch_small(ctx->h_misc, ctx->cstart + ctx->g.ncell, sizeof(int), ctx->stream);
     ctx->launches += 1;
     CHECK_LAUNCH(ctx);
@@ -457,6 +457,7 @@ int fsim_create(const fsim_grid_desc* gd, const fsim_params* params, fsim_ctx** 
     cudaMemset(ctx->count, 0, nc * 4);
     cudaMemset(ctx->cstart, 0, (nc + 1) * 4);
     cudaMemset(ctx->d_err, 0, sizeof(unsigned));
+    cudaMemset(ctx->d_misc, 0, 64);  // [0..1]: P2G work counters (each launch leaves them at zero)
     k_init_flags<<<ceil_div(g.ncell, 256), 256, 0, ctx->stream>>>(g, ctx->prm.top_solid, ctx->flags);
     if (solver_alloc(ctx) != FSIM_OK) return fail(FSIM_E_OOM, "solver allocation");
     if (!make_tensor_maps(ctx)) return fail(FSIM_E_CUDA, "tensor maps");

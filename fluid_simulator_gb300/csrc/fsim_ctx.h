@@ -155,8 +155,10 @@ struct AdvectArgs {
 };
 void launch_advect(const AdvectArgs& a, cudaStream_t s);
 void launch_scan(const int* in, int* out, long long n, int* block_sums, cudaStream_t s);
+// perm[cstart[key] + rank] = index, then each cell's segment in ascending
+// particle index (two kernels when n > 0)
 void launch_scatter(const uint32_t* key, const uint32_t* rank, const int* cstart, uint32_t* perm,
-                    long long n, cudaStream_t s);
+                    long long n, long long ncell, cudaStream_t s);
 void launch_gather(ParticleBuf src, ParticleBuf dst, const uint32_t* perm, const int* cstart,
                    long long ncell, long long n, bool ids, cudaStream_t s);
 void launch_spawn_sphere(ParticleBuf p, long long first, int count, const fsim_obstacle& o,

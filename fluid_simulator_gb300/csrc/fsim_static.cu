@@ -139,7 +139,7 @@ extern "C" int fsim_p2g_noalloc(const fsim_grid_desc* grid, int transfer, const 
         launch_advect(a, s);
     }
     launch_scan(count, cstart, g.ncell, blocks, s);
-    launch_scatter(key, rank, cstart, perm, n, s);
+    launch_scatter(key, rank, cstart, perm, n, g.ncell, s);
     float* const u[3] = {vx, vy, vz};
     if (launch_p2g_raw(p, perm, cstart, g, u, flags, avg, transfer == FSIM_APIC, s) != cudaSuccess)
         return FSIM_E_CUDA;

@@ -369,6 +369,63 @@ __global__ void k_scatter(const uint32_t* key, const uint32_t* rank, const int* 
     perm[cstart[k] + rank[i]] = (uint32_t)i;
 }
 
+// Stable cell order: the scatter places a cell's particles in the order their
+// warps won the count atomics, which varies from run to run.  This pass sorts
+// every cell's segment of perm by particle index, so the order inside a cell is
+// the order of the particle buffer (itself the previous step's cell order) and
+// every later sum over a cell's particles is reproducible.  Segments are
+// usually in order already (a cell's particles mostly share a warp); the
+// others of up to 16 entries go through a bitonic network in registers, longer
+// ones through an insertion sort in place.
+__device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b, bool up) {
+    const uint32_t lo = min(a, b), hi = max(a, b);
+    a = up ? lo : hi;
+    b = up ? hi : lo;
+}
+
+__global__ void k_cell_order(uint32_t* perm, const int* cstart, long long ncell) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int beg = cstart[c], end = cstart[c + 1];
+    const int len = end - beg;
+    if (len < 2) return;
+    bool sorted = true;
+    uint32_t prev = perm[beg];
+    for (int k = beg + 1; k < end; k++) {
+        const uint32_t x = perm[k];
+        sorted &= prev < x;
+        prev = x;
+    }
+    if (sorted) return;
+    if (len <= 16) {
+        uint32_t v[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) v[k] = k < len ? perm[beg + k] : 0xFFFFFFFFu;
+#pragma unroll
+        for (int size = 2; size <= 16; size <<= 1)
+#pragma unroll
+            for (int stride = size >> 1; stride > 0; stride >>= 1)
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                    const int l = k ^ stride;
+                    if (l > k) cswap(v[k], v[l], (k & size) == 0);
+                }
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            if (k < len) perm[beg + k] = v[k];
+        return;
+    }
+    for (int k = beg + 1; k < end; k++) {
+        const uint32_t x = perm[k];
+        int j = k - 1;
+        while (j >= beg && perm[j] > x) {
+            perm[j + 1] = perm[j];
+            j--;
+        }
+        perm[j + 1] = x;
+    }
+}
+
 // dst[j] = src[perm[j]] for the j < cstart[ncell] live particles
 __global__ void k_gather(ParticleBuf src, ParticleBuf dst, const uint32_t* perm, const int* cstart,
                          long long ncell, long long n, int ids) {
@@ -514,9 +571,10 @@ void launch_push_apart(ParticleBuf p, const uint32_t* perm, const int* cstart, c
 }
 
 void launch_scatter(const uint32_t* key, const uint32_t* rank, const int* cstart, uint32_t* perm,
-                    long long n, cudaStream_t s) {
+                    long long n, long long ncell, cudaStream_t s) {
     if (n <= 0) return;
     k_scatter<<<ceil_div(n, 256), 256, 0, s>>>(key, rank, cstart, perm, n);
+    k_cell_order<<<ceil_div(ncell, 256), 256, 0, s>>>(perm, cstart, ncell);
 }
 
 void launch_gather(ParticleBuf src, ParticleBuf dst, const uint32_t* perm, const int* cstart,

@@ -22,6 +22,8 @@
 // applies the cell sort to the particle arrays as a side effect.
 #include <cudaTypedefs.h>
 
+#include <algorithm>
+
 #include "fsim_ctx.h"
 
 namespace {
