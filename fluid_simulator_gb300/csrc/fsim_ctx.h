@@ -46,7 +46,8 @@ struct MGLevelBufs {
 };
 
 struct SolverBufs {
-    double conv_rate = 0.0;    // measured PCG residual-norm factor per iteration (chunk planning)
+    double conv_rate[2] = {0.0, 0.0};  // measured PCG residual-norm factor per iteration, per
+                                       // preconditioner (RB-IC, multigrid): chunk planning
     int nbx, nby, nbz;         // bricks per axis
     long long nbricks;
     int4* brick_xyz = nullptr; // active bricks (contain a fluid cell), ascending: {bx, by, bz, b}
@@ -69,9 +70,14 @@ struct SolverBufs {
     double last_scale = 1.0;      // dt / (rho h^2) of the last solve
     std::vector<MGLevelBufs> mg;  // multigrid hierarchy (built at allocation)
     int mg_cluster = 0;           // CTAs in the coarse-V-cycle cluster (0: separate launches)
-    cudaGraphExec_t iter_exec = nullptr;  // one PCG iteration, captured on first use
-    int iter_key = -1;                    // configuration the graph was captured for
-    int iter_kernels = 0;                 // kernels in that graph
+    // one PCG iteration as a CUDA graph, captured on first use per configuration
+    // (precision, preconditioner, sweep counts); up to four are kept
+    static constexpr int kIterGraphs = 4;
+    cudaGraphExec_t iter_exec[kIterGraphs] = {};
+    int iter_key[kIterGraphs] = {-1, -1, -1, -1};
+    int iter_kernels[kIterGraphs] = {};
+    long long iter_used[kIterGraphs] = {};  // last use (for replacement)
+    long long iter_clock = 0;
 };
 
 struct fsim_ctx {

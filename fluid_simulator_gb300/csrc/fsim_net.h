@@ -47,7 +47,7 @@ int launch_conv_wgrad(const WgradLaunch& L, cudaStream_t s);
 // Levels 0..3 with 16, 32, 64, 64 channels; two 3x3x3 conv + ReLU per level,
 // 2x2x2 stride-2 down-convolutions (space-to-depth + pointwise), trilinear 2x
 // up-sampling with skip concatenation, a 1x1x1 head to one channel.
-enum { NET_LAYERS = 17 };
+enum { NET_LAYERS = 17, NET_MAX_BATCH = 64 };
 
 struct NetLayer {
     int taps, cin, cout;
@@ -90,9 +90,12 @@ struct fsim_net {
     float* out = nullptr;         // [vox] FP32 prediction
     float* res = nullptr;         // [vox] residual of the prediction (training)
     float* gout = nullptr;        // [vox] loss gradient w.r.t. the prediction (training)
-    float loss_mse_weight = 0.01f;
-    double* d_loss = nullptr;     // loss accumulator
-    int* d_count = nullptr;       // fluid voxels in the batch
+    float* batch_target = nullptr;  // [vox] training batch target (fsim_net_train_batch)
+    uint8_t* batch_mask = nullptr;  // [vox] training batch fluid mask
+    float loss_l2_weight = 0.1f;    // weight of the relative L2 term of the loss
+    double* d_loss = nullptr;     // loss of the last backward pass
+    double* d_sums = nullptr;     // per sample: sum r^2, e^2, target^2, b^2
+    float* d_coef = nullptr;      // per sample: gradient factors of the two loss terms
     double* d_rms = nullptr;      // solver hook: sum b^2, count
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::string err;

@@ -63,12 +63,6 @@ __global__ void k_to_f32(const bf16* in, long long n, float* out) {
     if (i < n) out[i] = __bfloat162float(in[i]);
 }
 
-__global__ void k_count_mask(const uint8_t* mask, long long vox, int* count) {
-    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned bal = __ballot_sync(0xffffffffu, v < vox && mask[v] != 0);
-    if ((threadIdx.x & 31) == 0 && bal) atomicAdd(count, __popc(bal));
-}
-
 // ---- space-to-depth (2x2x2 stride-2 down-convolution = s2d + pointwise) -----
 // dst[coarse][(sd*4 + sh*2 + sw)*C + c] = src[2*coarse + (sd, sh, sw)][c]
 __global__ void k_s2d(const bf16* src, int ss, int so, int C, int n, int D, int H, int W, bf16* dst) {
@@ -218,24 +212,31 @@ __global__ void k_head(const bf16* d0, long long vox, const float* wgt, const fl
     out[v] = scale * s;
 }
 
-// ---- loss: residual of the guess in the solver's operator + weighted MSE --------
-// e = (out - target) on fluid voxels, r = A e with A the 7-point operator of the
-// cell types (diagonal: non-solid neighbours; -1 per fluid neighbour; voxels
-// outside the volume count as solid).  Since A target = rhs, r is the residual
-// the guess would leave in PCG.  loss = (sum r^2 + lam * sum e^2) / count.
+// ---- loss: relative residual of the guess + weighted relative L2 error -------
+// Per sample s of the batch, with e = out - target on the fluid voxels (mask),
+// A the solver's 7-point operator of the sample's cell types (diagonal: the
+// non-solid neighbours; -1 per fluid neighbour; voxels outside the volume
+// count as solid) and b the scaled rhs (input channel 0): since A target = b,
+// r = A e is the residual b - A out the guess leaves in PCG, and
+//   L_s = ||r|| / ||b|| + lam ||e|| / ||target||,   loss = mean_s L_s.
+// Pass 1 stores r and adds the per-sample sums of r^2, e^2, target^2, b^2;
+// k_loss_coef turns them into the loss and the per-sample gradient factors;
+// pass 2 writes dloss/dout = c_r A r + c_e e.  Warps never straddle two
+// samples (each sample's voxel count is a multiple of 512).
 __device__ __forceinline__ bool vox_solid(const bf16* x0, long long v) { return __bfloat162float(x0[v * 16 + 2]) > 0.5f; }
 
 template <bool GRAD>
 __global__ void k_loss(const float* out, const float* target, const uint8_t* mask, const bf16* x0, int n, int D,
-                       int H, int W, const int* count, float lam, float* r, float* gout, double* loss) {
-    const long long vox = (long long)n * D * H * W;
+                       int H, int W, float* r, float* gout, double* sums, const float* coef) {
+    const long long per = (long long)D * H * W;
+    const long long vox = (long long)n * per;
     const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    double l = 0.0;
+    double q[4] = {0.0, 0.0, 0.0, 0.0};
+    const int smp = (int)(min(v, vox - 1) / per);
     if (v < vox && mask[v]) {
         const int w = (int)(v % W), h = (int)((v / W) % H), d = (int)((v / ((long long)W * H)) % D);
         const long long off[6] = {1, -1, W, -(long long)W, (long long)W * H, -(long long)W * H};
         const bool in[6] = {w + 1 < W, w > 0, h + 1 < H, h > 0, d + 1 < D, d > 0};
-        const float cnt = (float)max(*count, 1);
         int ns = 0;
         float nb = 0.f;
         const float ev = out[v] - target[v];
@@ -247,20 +248,66 @@ __global__ void k_loss(const float* out, const float* target, const uint8_t* mas
             if (mask[u]) nb += GRAD ? r[u] : out[u] - target[u];
         }
         if (GRAD) {
-            gout[v] = 2.f / cnt * ((float)ns * r[v] - nb + lam * ev);
+            gout[v] = coef[2 * smp] * ((float)ns * r[v] - nb) + coef[2 * smp + 1] * ev;
         } else {
             const float rv = (float)ns * ev - nb;
+            const float bv = __bfloat162float(x0[v * 16]);
             r[v] = rv;
-            l = ((double)rv * rv + (double)lam * ev * ev) / cnt;
+            q[0] = (double)rv * rv;
+            q[1] = (double)ev * ev;
+            q[2] = (double)target[v] * target[v];
+            q[3] = (double)bv * bv;
         }
     } else if (v < vox) {
         if (GRAD) gout[v] = 0.f;
         else r[v] = 0.f;
     }
     if (!GRAD) {
-        for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
-        if ((threadIdx.x & 31) == 0 && l != 0.0) atomicAdd(loss, l);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            for (int o = 16; o > 0; o >>= 1) q[k] += __shfl_xor_sync(0xffffffffu, q[k], o);
+            if ((threadIdx.x & 31) == 0 && q[k] != 0.0) atomicAdd(&sums[4 * smp + k], q[k]);
+        }
     }
+}
+
+// Loss and gradient factors from the per-sample sums (one warp).  A sample
+// whose residual, error, target or rhs is zero contributes nothing to that term.
+__global__ void k_loss_coef(const double* sums, int n, float lam, float* coef, double* loss, float* loss_out) {
+    double l = 0.0;
+    for (int s = threadIdx.x; s < n; s += 32) {
+        const double rr = sums[4 * s], ee = sums[4 * s + 1], tt = sums[4 * s + 2], bb = sums[4 * s + 3];
+        const double nr = sqrt(rr), nb = sqrt(bb), ne = sqrt(ee), nt = sqrt(tt);
+        const bool res_ok = nr > 0.0 && nb > 0.0, err_ok = ne > 0.0 && nt > 0.0;
+        coef[2 * s] = res_ok ? (float)(1.0 / (n * nr * nb)) : 0.f;
+        coef[2 * s + 1] = err_ok ? (float)(lam / (n * ne * nt)) : 0.f;
+        l += (res_ok ? nr / nb : 0.0) + (err_ok ? lam * ne / nt : 0.0);
+    }
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+    if (threadIdx.x == 0) {
+        *loss = l / n;
+        if (loss_out) *loss_out = (float)(l / n);
+    }
+}
+
+// Training batch from a resident pool: sample b of the batch is pool sample
+// idx[b].  types: 0 fluid (an unknown of the solve), 1 air, 2 solid; rhs and
+// target are the scaled rhs and pressure.  Writes x0 (16 channels: rhs, fluid,
+// solid, air, 0...), the batch target and the fluid mask.
+__global__ void k_gather_batch(const uint8_t* types, const float* rhs, const float* target, const int* idx,
+                               long long per, int batch, bf16* x0, float* tb, uint8_t* mb) {
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= per * batch) return;
+    const long long b = v / per, j = v - b * per;
+    const long long src = (long long)idx[b] * per + j;
+    const uint8_t t = types[src];
+    const float a[8] = {t == 0 ? rhs[src] : 0.f, t == 0 ? 1.f : 0.f, t == 2 ? 1.f : 0.f, t == 1 ? 1.f : 0.f,
+                        0.f, 0.f, 0.f, 0.f};
+    const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    st8(x0 + v * 16, a);
+    st8(x0 + v * 16 + 8, z);
+    tb[v] = t == 0 ? target[src] : 0.f;
+    mb[v] = t == 0 ? 1 : 0;
 }
 
 // head backward: gz = dloss/d(pre-activation of d0), head weight / bias gradients
@@ -518,10 +565,12 @@ int ensure_ws(fsim_net* net, int n, int d, int h, int w, bool train) {
     for (int i = 0; i < NACT; i++) aoff[i] = take((size_t)level_vox(s, kActL[i]) * kActC[i] * 2);
     if (train)
         for (int i = 0; i < NGRAD; i++) goff[i] = take((size_t)level_vox(s, kGradL[i]) * kGradC[i] * 2);
-    size_t res_off = 0, gout_off = 0;
+    size_t res_off = 0, gout_off = 0, tb_off = 0, mb_off = 0;
     if (train) {
         res_off = take((size_t)level_vox(s, 0) * 4);
         gout_off = take((size_t)level_vox(s, 0) * 4);
+        tb_off = take((size_t)level_vox(s, 0) * 4);
+        mb_off = take((size_t)level_vox(s, 0));
     }
     const size_t out_off = take((size_t)level_vox(s, 0) * 4);
     void* mem = nullptr;
@@ -541,6 +590,8 @@ int ensure_ws(fsim_net* net, int n, int d, int h, int w, bool train) {
     net->out = (float*)(base + out_off);
     net->res = train ? (float*)(base + res_off) : nullptr;
     net->gout = train ? (float*)(base + gout_off) : nullptr;
+    net->batch_target = train ? (float*)(base + tb_off) : nullptr;
+    net->batch_mask = train ? (uint8_t*)(base + mb_off) : nullptr;
     net->amap.resize(2 * NET_LAYERS);
     for (int l = 0; l < NET_LAYERS; l++) {
         const NetBuf& in = net->act[kIn[l]];
@@ -712,20 +763,21 @@ int d2s(fsim_net* net, int gs2d, int gcat, int cat, int off, int C, int out) {
     return FSIM_OK;
 }
 
-int net_backward(fsim_net* net, const float* target, const uint8_t* mask) {
+int net_backward(fsim_net* net, const float* target, const uint8_t* mask, float* loss_out = nullptr) {
     const long long vox = level_vox(net->shape, 0);
     const NetShape& sh = net->shape;
-    NET_TRY(cudaMemsetAsync(net->d_loss, 0, sizeof(double), net->stream));
+    if (sh.n > NET_MAX_BATCH) return fail(net, "training batch larger than 64 samples", FSIM_E_INVALID);
+    NET_TRY(cudaMemsetAsync(net->d_sums, 0, sizeof(double) * 4 * sh.n, net->stream));
     k_loss<false><<<nblk(vox), NT_THREADS, 0, net->stream>>>(net->out, target, mask, net->act[X0].p, sh.n, sh.d, sh.h,
-                                                             sh.w, net->d_count, net->loss_mse_weight, net->res,
-                                                             nullptr, net->d_loss);
+                                                             sh.w, net->res, nullptr, net->d_sums, nullptr);
+    k_loss_coef<<<1, 32, 0, net->stream>>>(net->d_sums, sh.n, net->loss_l2_weight, net->d_coef, net->d_loss,
+                                           loss_out);
     k_loss<true><<<nblk(vox), NT_THREADS, 0, net->stream>>>(net->out, target, mask, net->act[X0].p, sh.n, sh.d, sh.h,
-                                                            sh.w, net->d_count, net->loss_mse_weight, net->res,
-                                                            net->gout, nullptr);
+                                                            sh.w, net->res, net->gout, nullptr, net->d_coef);
     k_head_bwd<<<nblk(vox), NT_THREADS, 0, net->stream>>>(net->act[D0].p, net->gout, vox, net->theta + net->head_w,
                                                           net->out_scale, net->gbuf[GD0].p, net->grad + net->head_w,
                                                           net->grad + net->head_b);
-    net->launches += 3;
+    net->launches += 4;
     int rc;
     auto cb = [&](int l) { return (rc = conv_bwd(net, l)) == FSIM_OK; };
     if (!cb(16) || !cb(15)) return rc;
@@ -846,7 +898,9 @@ int fsim_net_create(uint64_t seed, float out_scale, fsim_net** out) {
     if (cudaMalloc(&net->theta, pb) != cudaSuccess || cudaMalloc(&net->grad, pb) != cudaSuccess ||
         cudaMalloc(&net->adam_m, pb) != cudaSuccess || cudaMalloc(&net->adam_v, pb) != cudaSuccess ||
         cudaMalloc(&net->d_err, 64) != cudaSuccess || cudaMalloc(&net->d_loss, 8) != cudaSuccess ||
-        cudaMalloc(&net->d_count, 8) != cudaSuccess || cudaMalloc(&net->d_rms, 16) != cudaSuccess)
+        cudaMalloc(&net->d_sums, sizeof(double) * 4 * NET_MAX_BATCH) != cudaSuccess ||
+        cudaMalloc(&net->d_coef, sizeof(float) * 2 * NET_MAX_BATCH) != cudaSuccess ||
+        cudaMalloc(&net->d_rms, 16) != cudaSuccess)
         return bad("parameter allocation");
     long long wtot = 0;
     for (int l = 0; l < NET_LAYERS; l++) wtot += ((long long)net->L[l].taps * net->L[l].cin * net->L[l].cout + 127) / 128 * 128;
@@ -898,7 +952,8 @@ int fsim_net_destroy(fsim_net* net) {
     cudaFree(net->adam_v);
     cudaFree(net->d_err);
     cudaFree(net->d_loss);
-    cudaFree(net->d_count);
+    cudaFree(net->d_sums);
+    cudaFree(net->d_coef);
     cudaFree(net->d_rms);
     cudaFree(net->wpool);
     if (net->stream) cudaStreamDestroy(net->stream);
@@ -963,9 +1018,6 @@ int fsim_net_backward(fsim_net* net, const float* target, const uint8_t* mask, f
         unstage(net, st);
         return rc;
     }
-    NET_TRY(cudaMemsetAsync(net->d_count, 0, sizeof(int), net->stream));
-    k_count_mask<<<nblk(vox), NT_THREADS, 0, net->stream>>>((const uint8_t*)sm.p, vox, net->d_count);
-    net->launches++;
     rc = net_backward(net, (const float*)st.p, (const uint8_t*)sm.p);
     unstage(net, st);
     unstage(net, sm);
@@ -979,10 +1031,28 @@ int fsim_net_backward(fsim_net* net, const float* target, const uint8_t* mask, f
     return FSIM_OK;
 }
 
-int fsim_net_set_loss(fsim_net* net, float mse_weight) {
-    if (!net || !(mse_weight >= 0.f)) return FSIM_E_INVALID;
-    net->loss_mse_weight = mse_weight;
+int fsim_net_set_loss(fsim_net* net, float l2_weight) {
+    if (!net || !(l2_weight >= 0.f)) return FSIM_E_INVALID;
+    net->loss_l2_weight = l2_weight;
     return FSIM_OK;
+}
+
+int fsim_net_train_batch(fsim_net* net, int d, int h, int w, const uint8_t* types, const float* rhs,
+                         const float* target, const int* idx, int batch, float lr, float* loss_out) {
+    if (!net || !types || !rhs || !target || !idx || batch <= 0 || batch > NET_MAX_BATCH || !(lr > 0.f))
+        return FSIM_E_INVALID;
+    int rc = ensure_ws(net, batch, d, h, w, true);
+    if (rc) return rc;
+    const long long per = (long long)d * h * w;
+    k_gather_batch<<<nblk(per * batch), NT_THREADS, 0, net->stream>>>(types, rhs, target, idx, per, batch,
+                                                                      net->act[X0].p, net->batch_target,
+                                                                      net->batch_mask);
+    net->launches++;
+    NET_TRY(cudaGetLastError());
+    if ((rc = net_forward(net))) return rc;
+    NET_TRY(cudaMemsetAsync(net->grad, 0, (size_t)net->nparams * 4, net->stream));
+    if ((rc = net_backward(net, net->batch_target, net->batch_mask, loss_out))) return rc;
+    return fsim_net_adam(net, lr);
 }
 
 int fsim_net_zero_grad(fsim_net* net) {

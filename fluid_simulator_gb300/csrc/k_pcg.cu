@@ -1914,7 +1914,8 @@ void solver_free(fsim_ctx* ctx) {
     cudaFree(S.brick_xyz); cudaFree(S.d_nactive); cudaFree(S.brick_flag); cudaFree(S.code);
     cudaFree(S.b); cudaFree(S.phi); cudaFree(S.r); cudaFree(S.r64); cudaFree(S.partials);
     cudaFree(S.counter); cudaFree(S.st); cudaFreeHost(S.st_host); cudaFree(S.guess);
-    if (S.iter_exec) cudaGraphExecDestroy(S.iter_exec);
+    for (int k = 0; k < SolverBufs::kIterGraphs; k++)
+        if (S.iter_exec[k]) cudaGraphExecDestroy(S.iter_exec[k]);
     for (size_t l = 0; l < S.mg.size(); l++) {
         cudaFree(S.mg[l].r);
         if (l > 0) {
@@ -2020,23 +2021,36 @@ static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, int prec
     };
     const int key = (int)sizeof(T) * 10000000 + (mg ? 1000000 : 0) + ctx->prm.mg_sweeps * 10000 +
                     ctx->prm.mg_coarse_sweeps * 100 + ctx->prm.mg_cluster_sweeps;
-    if (S.iter_exec == nullptr || S.iter_key != key) {
-        if (S.iter_exec) {
-            cudaGraphExecDestroy(S.iter_exec);
-            S.iter_exec = nullptr;
+    int gi = -1;
+    for (int k = 0; k < SolverBufs::kIterGraphs; k++)
+        if (S.iter_exec[k] && S.iter_key[k] == key) gi = k;
+    if (gi < 0) {
+        // a free slot, else the least recently used one
+        gi = 0;
+        for (int k = 0; k < SolverBufs::kIterGraphs; k++) {
+            if (!S.iter_exec[k]) { gi = k; break; }
+            if (S.iter_used[k] < S.iter_used[gi]) gi = k;
+        }
+        if (S.iter_exec[gi]) {
+            cudaGraphExecDestroy(S.iter_exec[gi]);
+            S.iter_exec[gi] = nullptr;
         }
         const long long l0 = ctx->launches;
         cudaGraph_t graph = nullptr;
         FSIM_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         enqueue_iteration();
         FSIM_CUDA_TRY(ctx, cudaStreamEndCapture(st, &graph));
-        cudaError_t ie = cudaGraphInstantiate(&S.iter_exec, graph, 0);
+        cudaError_t ie = cudaGraphInstantiate(&S.iter_exec[gi], graph, 0);
         cudaGraphDestroy(graph);
         FSIM_CUDA_TRY(ctx, ie);
-        S.iter_key = key;
-        S.iter_kernels = (int)(ctx->launches - l0);
+        S.iter_key[gi] = key;
+        S.iter_kernels[gi] = (int)(ctx->launches - l0);
         ctx->launches = l0;
     }
+    S.iter_used[gi] = ++S.iter_clock;
+    cudaGraphExec_t iter_exec = S.iter_exec[gi];
+    const int iter_kernels = S.iter_kernels[gi];
+    double& conv_rate = S.conv_rate[mg ? 1 : 0];
     // Iterations are launched in chunks between host reads of the state.  The
     // chunk is the number of iterations the measured convergence rate (residual
     // norm factor per iteration, carried over from earlier solves) needs to reach
@@ -2045,7 +2059,7 @@ static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, int prec
     const int chunk_cap = mg ? 16 : 64;
     auto plan = [&]() -> int {
         const PcgState& h = *S.st_host;
-        const double rate = S.conv_rate;
+        const double rate = conv_rate;
         if (!(rate > 0.0 && rate < 1.0)) return mg ? 2 : 4;
         const double lr = std::log(rate);
         double n = 1e9;
@@ -2063,15 +2077,15 @@ static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, int prec
     double rr_mark = S.st_host->rr;
     while (!S.st_host->done && !S.st_host->nan) {
         for (int k = 0; k < chunk; k++) {
-            FSIM_CUDA_TRY(ctx, cudaGraphLaunch(S.iter_exec, st));
-            ctx->launches += S.iter_kernels;
+            FSIM_CUDA_TRY(ctx, cudaGraphLaunch(iter_exec, st));
+            ctx->launches += iter_kernels;
         }
         if ((rc = read_state())) return rc;
         PcgState& h = *S.st_host;
         if (h.nan) break;
         if (h.it > it_mark && rr_mark > 0.0 && h.rr > 0.0 && h.rr < rr_mark) {
             const double r = std::pow(h.rr / rr_mark, 0.5 / (h.it - it_mark));
-            S.conv_rate = S.conv_rate > 0.0 ? 0.5 * (S.conv_rate + r) : r;
+            conv_rate = conv_rate > 0.0 ? 0.5 * (conv_rate + r) : r;
         }
         it_mark = h.it;
         rr_mark = h.rr;

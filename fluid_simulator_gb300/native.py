@@ -114,7 +114,8 @@ EXPORTS = [
     "fsim_set_pressure_guess", "fsim_solve_pressure", "fsim_solve_current", "fsim_p2g_noalloc",
     "fsim_net_create", "fsim_net_destroy", "fsim_net_last_error", "fsim_net_num_params",
     "fsim_net_get_params", "fsim_net_set_params", "fsim_net_forward", "fsim_net_backward",
-    "fsim_net_set_loss", "fsim_net_zero_grad", "fsim_net_adam", "fsim_net_train_step", "fsim_net_synchronize",
+    "fsim_net_set_loss", "fsim_net_train_batch", "fsim_net_zero_grad", "fsim_net_adam", "fsim_net_train_step",
+    "fsim_net_synchronize",
     "fsim_net_conv", "fsim_set_net",
     "fsim_render_default_params", "fsim_render_camera", "fsim_render_create", "fsim_render_destroy",
     "fsim_render_last_error", "fsim_render_frame", "fsim_render_ctx", "fsim_render_read", "fsim_render_stats",
@@ -168,6 +169,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "fsim_net_forward": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_int]),
         "fsim_net_backward": (C.c_int, [P, P, P, fp, C.c_int]),
         "fsim_net_set_loss": (C.c_int, [P, C.c_float]),
+        "fsim_net_train_batch": (C.c_int, [P, C.c_int, C.c_int, C.c_int, P, P, P, P, C.c_int, C.c_float, P]),
         "fsim_net_zero_grad": (C.c_int, [P]),
         "fsim_net_adam": (C.c_int, [P, C.c_float]),
         "fsim_net_train_step": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, C.c_float, fp,
@@ -409,6 +411,7 @@ class WarmStartNet:
     def __init__(self, seed: int = 1, out_scale: float = 1.0):
         self.lib = load_library()
         self.net = C.c_void_p()
+        self.out_scale = float(out_scale)
         rc = self.lib.fsim_net_create(seed, out_scale, C.byref(self.net))
         if rc != 0:
             raise FsimError(f"fsim_net_create failed: {ERRORS.get(rc, rc)}")
@@ -466,8 +469,21 @@ class WarmStartNet:
         self._check(self.lib.fsim_net_backward(self.net, t, m, C.byref(loss), where), "fsim_net_backward")
         return loss.value
 
-    def set_loss(self, mse_weight: float):
-        self._check(self.lib.fsim_net_set_loss(self.net, mse_weight), "fsim_net_set_loss")
+    def set_loss(self, l2_weight: float):
+        self._check(self.lib.fsim_net_set_loss(self.net, l2_weight), "fsim_net_set_loss")
+
+    def train_batch(self, types, rhs, target, idx, lr: float, loss_out=None):
+        """One Adam step on pool samples idx (CUDA tensors: types uint8, rhs and
+        target float32 [samples, d, h, w], idx int32 [batch]); no host sync."""
+        d, h, w = types.shape[1:4]
+        self._check(self.lib.fsim_net_train_batch(self.net, d, h, w, C.c_void_p(types.data_ptr()),
+                                                  C.c_void_p(rhs.data_ptr()), C.c_void_p(target.data_ptr()),
+                                                  C.c_void_p(idx.data_ptr()), int(idx.shape[0]), lr,
+                                                  None if loss_out is None else C.c_void_p(loss_out.data_ptr())),
+                    "fsim_net_train_batch")
+
+    def synchronize(self):
+        self._check(self.lib.fsim_net_synchronize(self.net), "fsim_net_synchronize")
 
     def zero_grad(self):
         self._check(self.lib.fsim_net_zero_grad(self.net), "fsim_net_zero_grad")

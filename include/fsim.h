@@ -402,15 +402,26 @@ int fsim_net_set_params(fsim_net *net, const float *src, int where);
 /* Forward pass; train != 0 keeps what fsim_net_backward needs.  out may be NULL. */
 int fsim_net_forward(fsim_net *net, int n, int d, int h, int w, const float *in, float *out, int train,
                      int where);
-/* Backward pass after a training forward pass; adds to the gradient.  target
- * [n][d][h][w] FP32 is the plain solver's solution, mask (uint8) marks the
- * fluid cells.  With e = prediction - target on fluid cells and A the solver's
- * 7-point operator of the input's cell types (A target = rhs), the loss is
- * (sum (A e)^2 + mse_weight * sum e^2) / fluid cells: the residual the guess
- * leaves in PCG, plus a small error term for the smooth part. */
+/* Backward pass after a training forward pass (batch n <= 64); adds to the
+ * gradient.  target [n][d][h][w] FP32 is the plain solver's solution, mask
+ * (uint8) marks the fluid cells.  Per sample, with e = prediction - target on
+ * fluid cells, A the solver's 7-point operator of the input's cell types and
+ * b the scaled rhs (input channel 0; A target = b, so A e is the residual the
+ * guess leaves in PCG), the loss is the mean over the batch of
+ *   ||A e|| / ||b|| + l2_weight * ||e|| / ||target||
+ * (relative residual plus relative L2 error to the solver's pressure). */
 int fsim_net_backward(fsim_net *net, const float *target, const uint8_t *mask, float *loss, int where);
-/* mse_weight of the loss (default 0.01). */
-int fsim_net_set_loss(fsim_net *net, float mse_weight);
+/* l2_weight of the loss (default 0.1). */
+int fsim_net_set_loss(fsim_net *net, float l2_weight);
+/* One Adam step on a batch drawn from a training pool resident in device
+ * memory, without synchronising the host: sample b of the batch is pool
+ * sample idx[b] (device int array of `batch` entries, batch <= 64).  Pool
+ * arrays hold [samples][d][h][w]: types (uint8: 0 fluid unknown, 1 air,
+ * 2 solid), rhs and target (FP32, scaled as for fsim_net_forward / backward).
+ * loss_out (device float, may be NULL) receives the batch loss when the step
+ * has run; errors of the tensor-core kernels surface at fsim_net_synchronize. */
+int fsim_net_train_batch(fsim_net *net, int d, int h, int w, const uint8_t *types, const float *rhs,
+                         const float *target, const int *idx, int batch, float lr, float *loss_out);
 int fsim_net_zero_grad(fsim_net *net);
 /* Adam (beta 0.9 / 0.999, eps 1e-8) on the accumulated gradient, which it clears. */
 int fsim_net_adam(fsim_net *net, float lr);

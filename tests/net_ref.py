@@ -114,7 +114,10 @@ def operator(e: torch.Tensor, m: torch.Tensor, solid: torch.Tensor) -> torch.Ten
     return m * (ns * e - nb)
 
 
-def loss_and_grad(theta_np, x_np, t_np, m_np, out_scale: float = 1.0, mse_weight: float = 0.01, bf16: bool = True):
+def loss_and_grad(theta_np, x_np, t_np, m_np, out_scale: float = 1.0, l2_weight: float = 0.1, bf16: bool = True):
+    """Loss of fsim_net_backward: mean over samples of ||A e|| / ||b|| +
+    l2_weight ||e|| / ||target|| (b = input channel 0 as the kernels store it,
+    in BF16)."""
     theta = torch.tensor(theta_np, dtype=torch.float32, requires_grad=True)
     x = torch.tensor(x_np, dtype=torch.float32)
     t = torch.tensor(t_np, dtype=torch.float32)
@@ -122,6 +125,10 @@ def loss_and_grad(theta_np, x_np, t_np, m_np, out_scale: float = 1.0, mse_weight
     out = forward(theta, x, out_scale, bf16=bf16)
     e = (out - t) * m
     r = operator(e, m, x[..., 2])
-    loss = ((r * r).sum() + mse_weight * (e * e).sum()) / m.sum().clamp(min=1)
+    b = x[..., 0].bfloat16().float() * m
+    tm = t * m
+    dims = (1, 2, 3)
+    loss = (r.pow(2).sum(dims).sqrt() / b.pow(2).sum(dims).sqrt()
+            + l2_weight * e.pow(2).sum(dims).sqrt() / tm.pow(2).sum(dims).sqrt()).mean()
     loss.backward()
     return float(loss.detach()), out.detach().numpy(), theta.grad.numpy()

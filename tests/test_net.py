@@ -208,6 +208,35 @@ def test_adam_step_matches_formula(gpu):
 
 
 @pytest.mark.gpu
+def test_train_batch_equals_forward_backward_adam(gpu):
+    """fsim_net_train_batch (batch gathered on the device from a resident pool,
+    no host sync) makes the same Adam step as fsim_net_forward + backward + adam
+    on the same samples."""
+    import torch
+
+    from fluid_simulator_gb300 import native as N
+    from fluid_simulator_gb300 import warmstart as W
+    x, t, m = _batch(5, 16, 40)
+    pool = W.pool_from_arrays(x, t, m)
+    idx = torch.tensor([3, 0, 3], dtype=torch.int32, device="cuda")
+    a = N.WarmStartNet(seed=2)
+    b = N.WarmStartNet(seed=2)
+    theta = _random_head(a)
+    b.set_params(theta)
+    loss_d = torch.zeros(1, dtype=torch.float32, device="cuda")
+    a.train_batch(*pool, idx, 1e-3, loss_d)
+    a.synchronize()
+    sel = [3, 0, 3]
+    lb = b.train_step(x[sel], t[sel], m[sel], 1e-3)
+    assert abs(float(loss_d.item()) - lb) <= 1e-5 * abs(lb)
+    pa, pb = a.params(), b.params()
+    assert np.abs(pa - pb).max() <= 1e-6 * max(1.0, np.abs(pb).max())
+    assert not np.array_equal(pa, theta)
+    a.close()
+    b.close()
+
+
+@pytest.mark.gpu
 def test_training_and_learned_guess_gain(gpu):
     """Train on plain-solver pairs; the judged learned guess must beat the zero start."""
     from fluid_simulator_gb300 import native as N
@@ -217,7 +246,9 @@ def test_training_and_learned_guess_gain(gpu):
     xs, ts, ms = W.make_dataset(n, 48, seed=1, solver=solver)
     net = N.WarmStartNet(seed=1, out_scale=W.target_scale(ts, ms))
     hist = W.train(net, xs, ts, ms, iters=600, batch=8, lr=1e-3)
-    assert np.mean(hist[-20:]) < 0.5 * np.mean(hist[:20])
+    # the loss (relative residual + 0.1 relative error) starts at 1.1 for the zero guess
+    assert abs(np.mean(hist[:5]) - 1.1) < 0.05
+    assert np.mean(hist[-20:]) < 0.75 * np.mean(hist[:20])
     solver.sim.set_net(net)
     print("loss", np.mean(hist[:10]), "->", np.mean(hist[-10:]))
     its_zero, its_learned, used = [], [], 0
