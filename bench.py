@@ -358,7 +358,7 @@ def run_fsim(args):
         "gpu_launches": int(sum(s.kernel_launches for s in stats)),
     }
     if args.precision_study:
-        line["pcg_precision"] = precision_study(sim, dt, N)
+        line["pcg_precision"] = precision_study(sim, N)
     if args.ws_steps > 0:
         line["pcg_warm_start"] = warm_start_study(sim, dt, t, h, N, args)
     if args.render:
@@ -526,25 +526,55 @@ def render_study(sim, N, h, peak):
 
 
 # ---------------------------------------------------------------- precision study
-def precision_study(sim, dt, N):
-    """The last step's pressure problem (256^3 rhs and cell types) solved in each
-    precision; errors against an FP64 PCG solution (RB-IC, FP64 vectors,
-    relative residual 1e-12), max over fluid cells relative to max |p|."""
-    flags = sim.grid(N.F_FLAGS)
-    rhs = sim.grid(N.F_DIVERGENCE).astype(np.float64)
-    fluid = flags == N.WATER
-    runs = [("fp64_rbic_1e-12", N.PREC_FP64, 1e-12), ("mixed_mg_1e-6", N.PREC_MIXED, 1e-6),
-            ("fp32_mg_1e-6", N.PREC_FP32, 1e-6), ("mixed_mg_1e-10", N.PREC_MIXED, 1e-10)]
-    out = {}
-    ref = None
-    for name, prec, tol in runs:
-        p, st = sim.solve_pressure(rhs, dt, precision=prec, tol_mode=N.TOL_REL_L2, tol=tol, max_iters=20000)
-        if ref is None:
-            ref = p
-        scale = max(np.abs(ref[fluid]).max(), 1e-300)
-        out[name] = {"iterations": st.pcg_iterations, "ms": round(st.ms_solve, 3),
-                     "residual_rel": st.residual_rel,
-                     "err_vs_fp64": float(np.abs(p - ref)[fluid].max() / scale)}
+def precision_study(sim, N, seed: int = 11):
+    """Pressure projection alone at 256^3: cell types from APIC dam-break
+    snapshots (after 30 and 60 steps) and from seeded random masks
+    (Gaussian-filtered N(0, 1) noise, sigma 6 cells, 40-70 % fluid, solid
+    walls); rhs the divergence of a seeded N(0, 1) face-velocity field smoothed
+    with sigma 3 cells.  Solvers: FP32 PCG with FP64 dots and scalars
+    (FSIM_PREC_FP32) and FP32 inner solves with FP64-residual refinement
+    (FSIM_PREC_MIXED), multigrid-preconditioned, at relative residuals 1e-4,
+    1e-6 and 1e-8, against the all-FP64 PCG (FSIM_PREC_FP64, red-black IC)
+    solved to 1e-10.  Error = max over fluid cells of |p - p_fp64| / max |p_fp64|;
+    time-to-tolerance = the solve's CUDA-event time."""
+    from fluid_simulator_gb300 import warmstart as W
+    from fluid_simulator_gb300.scenes import GridSpec, dam_break
+
+    res = sim.shape[0]
+    dt = 1.0 / float(res * res)  # dt / (rho h^2) = 1: rhs in the solver's units
+    problems = []
+    p = N.default_params(transfer=N.APIC, resolution=res, tol=1e-6, tol_mode=N.TOL_REL_L2, max_iters=2000)
+    ds = N.Simulation(res, p)
+    ds.set_particles(dam_break(GridSpec(res), seed=0))
+    for s in range(60):
+        ds.step(1.0 / 480.0)
+        if s + 1 in (30, 60):
+            problems.append((f"dam256_step{s + 1}", ds.grid(N.F_FLAGS)))
+    ds.close()
+    masks, _ = W.mask_problems(res, 2, seed)
+    problems += [(f"mask_seed{seed}_{i}", masks[i]) for i in range(2)]
+    rng = np.random.default_rng(seed + 1)
+    out = {"grid": [res] * 3, "reference": "FP64 PCG (red-black IC), relative residual 1e-10",
+           "preconditioner": "multigrid", "problems": {}}
+    keep = sim.params
+    for name, flags in problems:
+        rhs = np.where(flags == N.WATER, W.random_divergence(rng, 1, res)[0], 0.0).astype(np.float64)
+        sim.set_grid(N.F_FLAGS, flags)
+        ref, st = sim.solve_pressure(rhs, dt, precision=N.PREC_FP64, tol_mode=N.TOL_REL_L2, tol=1e-10,
+                                     max_iters=40000)
+        fluid = W.solver_fluid(flags)
+        scale = max(float(np.abs(ref[fluid]).max()), 1e-300)
+        row = {"fluid_cells": int(fluid.sum()), "fp64": {"iterations": st.pcg_iterations, "ms": round(st.ms_solve, 2),
+                                                         "residual_rel": float(f"{st.residual_rel:.3g}")}}
+        for pname, prec in (("mixed", N.PREC_MIXED), ("fp32", N.PREC_FP32)):
+            for tol in (1e-4, 1e-6, 1e-8):
+                pp, st = sim.solve_pressure(rhs, dt, precision=prec, tol_mode=N.TOL_REL_L2, tol=tol, max_iters=400)
+                row[f"{pname}_{tol:.0e}"] = {
+                    "iterations": st.pcg_iterations, "ms": round(st.ms_solve, 3), "converged": bool(st.converged),
+                    "residual_rel": float(f"{st.residual_rel:.3g}"),
+                    "err_vs_fp64": float(f"{float(np.abs(pp - ref)[fluid].max()) / scale:.3g}")}
+        out["problems"][name] = row
+    sim.set_params(keep)
     return out
 
 

@@ -243,13 +243,19 @@ def mask_problems(n: int, count: int, seed: int, threads: int = -1):
     flags[:, 0] = flags[:, -1] = N.SOLID
     flags[:, :, 0] = flags[:, :, -1] = N.SOLID
     flags[:, :, :, 0] = flags[:, :, :, -1] = N.SOLID
+    rhs = np.where(flags == N.WATER, random_divergence(rng, count, n, threads), 0.0).astype(np.float32)
+    return flags, rhs
+
+
+def random_divergence(rng, count: int, n: int, threads: int = -1) -> np.ndarray:
+    """-div of an N(0, 1) face-velocity field smoothed with sigma = 3 cells,
+    [count, n, n, n] float32 (the smoothing is applied to the divergence of the
+    white-noise field: the filter commutes with the difference operator)."""
     ux = rng.standard_normal((count, n + 1, n, n), dtype=np.float32)
     uy = rng.standard_normal((count, n, n + 1, n), dtype=np.float32)
     uz = rng.standard_normal((count, n, n, n + 1), dtype=np.float32)
     div = (ux[:, 1:] - ux[:, :-1]) + (uy[:, :, 1:] - uy[:, :, :-1]) + (uz[:, :, :, 1:] - uz[:, :, :, :-1])
-    div = _smooth_batch(div, 3.0, threads)
-    rhs = np.where(flags == N.WATER, -div, 0.0).astype(np.float32)
-    return flags, rhs
+    return -_smooth_batch(div, 3.0, threads)
 
 
 def crop_problem(flags: np.ndarray, rhs: np.ndarray, origin, n: int = PROTO_N):
