@@ -722,6 +722,37 @@ def cpu_baseline(res: int, dt: float, steps: int = 1, warm: int = 0):
             "seconds_per_step": round(sec, 3)}
 
 
+def run_solve_case(args):
+    """Pressure solves alone on the benchmark's cell types (fluid below y = 0.5
+    in the 256^3 box, solid walls) with a seeded random-divergence rhs and no
+    particles: the solver's kernels at the benchmark size with a few hundred MB
+    on the device, for counter captures.  Prints one JSON line."""
+    from fluid_simulator_gb300 import native as N
+    from fluid_simulator_gb300 import warmstart as W
+
+    res = args.res
+    p = N.default_params(transfer=N.APIC, resolution=res, tol=1e-6, tol_mode=N.TOL_REL_L2, max_iters=2000,
+                         timing=True, precond={"mg": N.PRECOND_MG, "rbic": N.PRECOND_RBIC}[args.precond])
+    sim = N.Simulation(res, p)
+    c = (np.arange(res) + 0.5) / res
+    flags = np.full((res, res, res), N.AIR, np.uint8)
+    flags[:, c < 0.5, :] = N.WATER
+    flags[0], flags[-1] = N.SOLID, N.SOLID
+    flags[:, 0], flags[:, -1] = N.SOLID, N.SOLID
+    flags[:, :, 0], flags[:, :, -1] = N.SOLID, N.SOLID
+    rhs = np.where(flags == N.WATER, W.random_divergence(np.random.default_rng(3), 1, res)[0], 0.0)
+    sim.set_grid(N.F_FLAGS, flags)
+    dt = 1.0 / float(res * res)
+    rec = []
+    for _ in range(args.solve_case):
+        _, st = sim.solve_pressure(rhs, dt, precision=N.PREC_MIXED, tol_mode=N.TOL_REL_L2, tol=1e-6, max_iters=2000)
+        rec.append((st.ms_solve, st.pcg_iterations))
+    sim.close()
+    print(json.dumps({"solve_case": {"grid": [res] * 3, "precond": args.precond, "fluid_cells": int((flags == 0).sum()),
+                                     "ms": [round(x[0], 3) for x in rec], "iterations": [x[1] for x in rec]}}),
+          flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -777,6 +808,8 @@ def main():
     ap.add_argument("--ws-steps", type=int, default=6,
                     help="problems per scene of the zero / previous / learned warm-start comparison (0: skip)")
     ap.add_argument("--render", type=int, default=1, help="time one 1000x1000 frame of the headless renderer")
+    ap.add_argument("--solve-case", type=int, default=0,
+                    help="only K pressure solves of the benchmark's cell types (no particles), for counter captures")
     ap.add_argument("--parity", type=int, default=1,
                     help="free-running drift curves against the oracle: 32^3 FLIP (100 steps, oracle run live) "
                          "and 128^3 PIC / FLIP / APIC (200 steps, oracle trajectories from tests/golden) (0: skip)")
@@ -784,7 +817,9 @@ def main():
                     help="mixed-precision refinement every 10^k residual drop (0: library default 3)")
     args = ap.parse_args()
     os.makedirs(args.out_dir, exist_ok=True)
-    if args.impl == "reference":
+    if args.solve_case > 0:
+        run_solve_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_fsim(args)
