@@ -287,6 +287,17 @@ def run_fsim(args):
     e2e_ms = ev.stop_ms()
     barrier(dist)
     e2e_ms = dist_max(dist, e2e_ms)
+    # one publish alone (gfx kernel + copy to the pinned host buffer), for the copy's own rate
+    pub = []
+    for _ in range(3):
+        sim.synchronize()
+        t0 = time.perf_counter()
+        got = C.c_int64()
+        sim.lib.fsim_fill_gfx_async(sim.ctx, gfx, n_cap, C.byref(got))
+        sim.lib.fsim_gfx_wait(sim.ctx)
+        pub.append(time.perf_counter() - t0)
+    pub_s = min(pub)
+    pub_bytes = got.value * C.sizeof(N.ParticleGfx)
     rt.cudaHostUnregister(C.cast(gfx, C.c_void_p))
 
     # per-stage breakdown (library events)
@@ -354,7 +365,10 @@ def run_fsim(args):
         "e2e": {"value": round(world * e2e_steps / (e2e_ms / 1000.0), 4), "unit": "steps/s",
                 "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps,
                 "steps": e2e_steps,
-                "path": "fsim_set_obstacles + fsim_step + fsim_fill_gfx_async(pinned host) per step, fsim_gfx_wait"},
+                "path": "fsim_set_obstacles + fsim_step + fsim_fill_gfx_async(pinned host) per step, fsim_gfx_wait",
+                "d2h_gbs_window": round(d2h / (e2e_ms / 1e3) / 1e9, 1),
+                "publish_alone_ms": round(pub_s * 1e3, 3),
+                "publish_alone_d2h_gbs": round(pub_bytes / pub_s / 1e9, 1)},
         "gpu_launches": int(sum(s.kernel_launches for s in stats)),
     }
     if args.precision_study:

@@ -315,6 +315,22 @@ int do_spawn(fsim_ctx* ctx, double dt) {
     if (total == 0) return FSIM_OK;
     int rc = ensure_capacity(ctx, ctx->n + total);
     if (rc) return rc;
+    // the step's disc cell lists go to mapped pinned memory (grown rarely); the
+    // previous step's spawn kernels finished before that step returned
+    long long list_ints = 0;
+    for (const auto& j : jobs) list_ints += (long long)j.cells.size();
+    if (list_ints > ctx->disc_cells_cap) {
+        if (ctx->disc_cells_host) cudaFreeHost(ctx->disc_cells_host);
+        ctx->disc_cells_host = nullptr;
+        ctx->disc_cells_dev = nullptr;
+        ctx->disc_cells_cap = 0;
+        const long long cap = std::max<long long>(2 * list_ints, 1024);
+        FSIM_CUDA_TRY(ctx, cudaHostAlloc((void**)&ctx->disc_cells_host, (size_t)cap * sizeof(int),
+                                         cudaHostAllocMapped));
+        FSIM_CUDA_TRY(ctx, cudaHostGetDevicePointer((void**)&ctx->disc_cells_dev, ctx->disc_cells_host, 0));
+        ctx->disc_cells_cap = cap;
+    }
+    long long list_off = 0;
     const bool ids = ctx->prm.track_ids != 0;
     for (auto& j : jobs) {
         const fsim_obstacle& o = ctx->obs[j.obs];
@@ -324,15 +340,11 @@ int do_spawn(fsim_ctx* ctx, double dt) {
                                 ids, ctx->stream);
             ctx->launches += 1;
         } else {
-            int* dcells = nullptr;
-            FSIM_CUDA_TRY(ctx, cudaMallocAsync(&dcells, j.cells.size() * sizeof(int), ctx->stream));
-            FSIM_CUDA_TRY(ctx, cudaMemcpyAsync(dcells, j.cells.data(), j.cells.size() * sizeof(int),
-                                               cudaMemcpyHostToDevice, ctx->stream));
-            launch_spawn_disc(ctx->buf[ctx->cur], ctx->n, (int)(j.cells.size() / 2), o, g, j.cy, dcells, seed,
-                              ctx->next_id, ids, ctx->stream);
+            std::memcpy(ctx->disc_cells_host + list_off, j.cells.data(), j.cells.size() * sizeof(int));
+            launch_spawn_disc(ctx->buf[ctx->cur], ctx->n, (int)(j.cells.size() / 2), o, g, j.cy,
+                              ctx->disc_cells_dev + list_off, seed, ctx->next_id, ids, ctx->stream);
+            list_off += (long long)j.cells.size();
             ctx->launches += 1;
-            FSIM_CUDA_TRY(ctx, cudaFreeAsync(dcells, ctx->stream));
-            FSIM_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // host vector lifetime
         }
         ctx->n += j.count;
         ctx->next_id += (uint32_t)j.count;
@@ -487,6 +499,7 @@ int fsim_destroy(fsim_ctx* ctx) {
     cudaFree(ctx->flags); cudaFree(ctx->valid); cudaFree(ctx->avg);
     for (int a = 0; a < 3; a++) { cudaFree(ctx->u[a]); cudaFree(ctx->v2[a]); }
     cudaFree(ctx->d_err); cudaFree(ctx->d_misc); cudaFreeHost(ctx->h_misc);
+    if (ctx->disc_cells_host) cudaFreeHost(ctx->disc_cells_host);
     solver_free(ctx);
     if (ctx->events)
         for (int k = 0; k < EV_COUNT; k++) cudaEventDestroy(ctx->ev[k]);

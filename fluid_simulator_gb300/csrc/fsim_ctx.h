@@ -123,6 +123,11 @@ struct fsim_ctx {
     // obstacles (host copy; sources carry last_spawn_fraction)
     std::vector<fsim_obstacle> obs;
     uint64_t spawn_counter = 0;
+    // disc-source cell lists of a step: mapped pinned host memory the spawn
+    // kernel reads directly (no copy-engine transfer inside a step)
+    int* disc_cells_host = nullptr;
+    int* disc_cells_dev = nullptr;
+    long long disc_cells_cap = 0;
 
     // TMA descriptors for the G2P tile loads (v2 x/y/z, v x/y/z)
     CUtensorMap tmap[6];
