@@ -234,6 +234,347 @@ __global__ void __launch_bounds__(P2G_THREADS, 2) k_p2g(const P2GArgs a) {
     }
 }
 
+// ---- P2G: x sweep over pencils, particle-parallel fixed-point accumulation ----
+//
+// The context path's P2G.  A work item is a pencil segment: FX_SY x FX_SZ
+// owned cells in (y, z) over FX_LX owned x-slices.  The CTA sweeps the
+// segment's slices in x (plus one halo slice at each end) and walks, in each
+// slice, the owned footprint and its one-cell ring (18 rows of 32 cells).
+// Contributions reach the neighbouring x-planes only, so three x-planes of
+// FP32 accumulators (7 fields over the owned footprint) live in shared memory
+// as a ring; after slice x, plane x - 1 is complete: it is normalised (v /
+// weight if weight > 1e-6, else 0; WATER where a particle is; avgPNum),
+// written out and cleared for plane x + 2.  Contributions outside the owned
+// footprint are dropped (the neighbouring pencil computes them from the same
+// ring particles): the walk is 1.2x the owned cells.
+//
+// A warp quad takes one walk row (32 cells, one contiguous run of the
+// cell-sorted order) at a time, in batches of up to FX_PCAP particles:
+//  * the quad stages the batch's particles into shared memory with coalesced
+//    loads, placing them rank-major (the first particle of every cell, then
+//    the second ...), so that the 32 lanes of a warp mostly hold particles of
+//    different cells and their atomic targets rarely meet;
+//  * every thread takes particles of the batch and adds each particle's 56
+//    contributions (8 faces x 3 axes, weight and weighted velocity, and 8
+//    density weights) to a row accumulator (3 x 3 x 34 cells around the row,
+//    7 fields) with INT32 shared-memory atomics in fixed point: weights scaled
+//    by 2^21, weighted velocities by 2^21 / 2^ceil(log2 Vmax) with Vmax the
+//    batch's largest |v_a| + h sum_b |c_ab| (the z term scaled by the 2D
+//    mode's cell aspect), so every term is below 2^21 in
+//    magnitude and a batch's sums stay below 2^29 -- no overflow, a rounding
+//    of 2^-21 of the batch's largest term, and integer sums that do not
+//    depend on the order of the atomics;
+//  * the batch's sums are converted back to FP32 and added to the plane ring
+//    with plain shared-memory adds.
+// Quad q handles walk rows 6q .. 6q + 5 in two phases of three rows (a CTA
+// barrier between phases), so rows handled at the same time are at least 5
+// apart and their plane targets (rows +-1) never meet: the plane ring gets
+// its contributions in a fixed order and P2G is reproducible bit for bit.
+// Particles with a non-finite position, velocity or C contribute nothing.
+//
+// Work items come from a counter (d_misc[0]); the last CTA to finish resets it
+// and the exit counter (d_misc[1]) for the next launch.
+constexpr int FX_SY = 16;             // owned y cells per pencil
+constexpr int FX_WZ = 32;             // walk cells per row
+constexpr int FX_SZ = FX_WZ - 2;      // owned z cells per pencil
+constexpr int FX_WY = FX_SY + 2;      // walk rows per slice
+constexpr int FX_LX = 32;             // owned x slices per work item
+constexpr int FX_QUADS = 3;
+constexpr int FX_THREADS = FX_QUADS * 128;
+constexpr int FX_PCAP = 192;          // particles per batch
+constexpr int FX_PLANE = FX_SY * FX_WZ;
+constexpr int FX_RZ = FX_WZ + 2;      // row accumulator z extent (z0 - 2 .. z0 + 31)
+constexpr int FX_RACC = 7 * 9 * FX_RZ;  // row accumulator entries (field, dx, dy, z)
+static_assert(FX_WY == 6 * FX_QUADS, "each quad takes six walk rows");
+
+template <bool APIC>
+__host__ __device__ constexpr int fx_fields() { return APIC ? 15 : 6; }
+// per-quad scratch (floats / ints): staged fields, cell of each staged slot,
+// rank tables, cell starts, warp maxima, row accumulator
+template <bool APIC>
+__host__ __device__ constexpr int fx_quad_words() {
+    return fx_fields<APIC>() * FX_PCAP + FX_PCAP + 2 * (FX_PCAP + 1) + 36 + 4 + FX_RACC;
+}
+template <bool APIC>
+constexpr int fx_smem() { return (3 * 7 * FX_PLANE + FX_QUADS * fx_quad_words<APIC>()) * 4; }
+
+struct P2GFxArgs {
+    ParticleBuf p;
+    const uint32_t* perm;
+    const int* cstart;
+    GridGeom g;
+    float* u[3];
+    uint8_t* flags;
+    float* avg;
+    int* work;          // [0] next item, [1] CTAs done
+    int nsx, npy, npz;  // segments in x, pencils in y and z
+    int nitems;
+};
+
+__device__ __forceinline__ void fx_quad_bar(int quad) {
+    asm volatile("bar.sync %0, 128;" ::"r"(quad + 1) : "memory");
+}
+
+// round(x) for |x| < 2^22: adding 1.5 * 2^23 leaves the integer in the low
+// mantissa bits
+__device__ __forceinline__ int fx_round(float x) { return __float_as_int(x + 12582912.0f) - 0x4B400000; }
+
+// 2^(21 - e) with 2^e the smallest power of two above vmax (vmax > 0, finite)
+__device__ __forceinline__ float fx_vscale(float vmax) {
+    int e;
+    frexpf(vmax, &e);  // vmax = m 2^e, 0.5 <= m < 1
+    return ldexpf(1.f, 21 - e);
+}
+
+template <bool APIC>
+__global__ void __launch_bounds__(FX_THREADS, 2) k_p2g_fx(const P2GFxArgs a) {
+    extern __shared__ float sm[];
+    constexpr int NF = fx_fields<APIC>();
+    float* planes = sm;                                        // [3 slots][7 fields][FX_PLANE]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int quad = warp >> 2, qw = warp & 3, qt = threadIdx.x & 127;
+    float* qbase = sm + 3 * 7 * FX_PLANE + quad * fx_quad_words<APIC>();
+    float* stage = qbase;                                      // [NF][FX_PCAP]
+    int* cellof = reinterpret_cast<int*>(stage + NF * FX_PCAP);  // [FX_PCAP] walk cell of a slot, -1 invalid
+    int* rank_off = cellof + FX_PCAP;                          // [FX_PCAP + 1] slots before rank r
+    unsigned* rank_mask = reinterpret_cast<unsigned*>(rank_off + FX_PCAP + 1);  // cells holding rank r
+    int* cs = reinterpret_cast<int*>(rank_mask + FX_PCAP + 1); // [33] batch-relative cell starts (+3 pad)
+    float* wmax = reinterpret_cast<float*>(cs + 36);           // [4] per-warp Vmax
+    int* racc = reinterpret_cast<int*>(wmax + 4);              // [7][3][3][FX_RZ]
+    __shared__ int s_item;
+    const GridGeom& g = a.g;
+    const float h = g.h, zr = g.two_d ? (float)(g.hzd * g.hinvd) : 1.f;
+    const float hinv3[3] = {g.hinv, g.hinv, g.hzinv};
+    const float WS = 2097152.f;  // 2^21
+
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(&a.work[0], 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= a.nitems) break;
+        const int pzi = item % a.npz, pyi = (item / a.npz) % a.npy, sxi = item / (a.npz * a.npy);
+        const int xa = sxi * FX_LX, xe = min(xa + FX_LX, g.nx);
+        const int y0 = pyi * FX_SY, z0 = pzi * FX_SZ;
+        const int ny_left = min(FX_SY, g.ny - y0), nz_left = min(FX_SZ, g.nz - z0);
+        for (int k = threadIdx.x; k < 3 * 7 * FX_PLANE; k += FX_THREADS) planes[k] = 0.f;
+        for (int k = qt; k < FX_RACC; k += 128) racc[k] = 0;
+        __syncthreads();
+        for (int x = xa - 1; x <= xe; x++) {
+            if (x >= 0 && x < g.nx) {
+                for (int phase = 0; phase < 2; phase++) {
+                    for (int rr = 0; rr < 3; rr++) {
+                        const int wy = quad * 6 + phase * 3 + rr;
+                        const int y = y0 - 1 + wy;
+                        if (y < 0 || y >= g.ny) continue;  // uniform across the quad
+                        const long long rowc = gidx(g, x, y, 0);
+                        const int zlo = max(z0 - 1, 0), zhi = min(z0 - 1 + FX_WZ, g.nz);
+                        const int rb = a.cstart[rowc + zlo], re = a.cstart[rowc + zhi];
+                        for (int bs = rb; bs < re; bs += FX_PCAP) {
+                            const int cnt = min(FX_PCAP, re - bs);
+                            // batch-relative cell starts of the 32 walk cells and the rank tables
+                            if (qw == 0) {
+                                const int z = z0 - 1 + lane;
+                                int c0 = 0, c1 = 0;
+                                if (z >= 0 && z < g.nz) {
+                                    c0 = min(max(a.cstart[rowc + z] - bs, 0), cnt);
+                                    c1 = min(max(a.cstart[rowc + z + 1] - bs, 0), cnt);
+                                } else {
+                                    c0 = c1 = z < 0 ? 0 : cnt;
+                                }
+                                cs[lane] = c0;
+                                if (lane == 31) cs[32] = cnt;
+                                const int c = c1 - c0;
+                                int maxc = c;
+#pragma unroll
+                                for (int o = 16; o > 0; o >>= 1) maxc = max(maxc, __shfl_xor_sync(0xffffffffu, maxc, o));
+                                int run = 0;
+                                for (int r = 0; r < maxc; r++) {
+                                    const unsigned m = __ballot_sync(0xffffffffu, c > r);
+                                    if (lane == 0) {
+                                        rank_mask[r] = m;
+                                        rank_off[r] = run;
+                                    }
+                                    run += __popc(m);
+                                }
+                            }
+                            fx_quad_bar(quad);
+                            // stage rank-major, with the batch's velocity bound
+                            float vm = 0.f;
+                            for (int j = qt; j < cnt; j += 128) {
+                                int lo = 0, hi = 32;  // the cell l with cs[l] <= j < cs[l + 1]
+#pragma unroll
+                                for (int step = 0; step < 5; step++) {
+                                    const int mid = (lo + hi) >> 1;
+                                    if (cs[mid] <= j) lo = mid;
+                                    else hi = mid;
+                                }
+                                const int l = lo;
+                                const int r = j - cs[l];
+                                const int slot = rank_off[r] + __popc(rank_mask[r] & ((1u << l) - 1u));
+                                const uint32_t i = a.perm[bs + j];
+                                float q[NF];
+#pragma unroll
+                                for (int d = 0; d < 3; d++) {
+                                    q[d] = a.p.p[d][i];
+                                    q[3 + d] = a.p.v[d][i];
+                                }
+                                if (APIC) {
+#pragma unroll
+                                    for (int k = 0; k < 9; k++) q[6 + k] = a.p.c[k][i];
+                                }
+                                bool ok = true;
+                                float pm = 0.f;
+#pragma unroll
+                                for (int d = 0; d < 3; d++) {
+                                    float m = fabsf(q[3 + d]);
+                                    // |c_d . (face - pos)| <= h sum_b |c_db| (z scaled by zr in 2D mode)
+                                    if (APIC)
+                                        m += h * (fabsf(q[6 + 3 * d]) + fabsf(q[7 + 3 * d]) + fabsf(q[8 + 3 * d]) * zr);
+                                    pm = fmaxf(pm, m);
+                                }
+#pragma unroll
+                                for (int k = 0; k < NF; k++) ok &= isfinite(q[k]);
+                                if (ok) vm = fmaxf(vm, pm);
+#pragma unroll
+                                for (int k = 0; k < NF; k++) stage[k * FX_PCAP + slot] = q[k];
+                                cellof[slot] = ok ? l : -1;
+                            }
+#pragma unroll
+                            for (int o = 16; o > 0; o >>= 1) vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+                            if (lane == 0) wmax[qw] = vm;
+                            fx_quad_bar(quad);
+                            const float vmax = fmaxf(fmaxf(wmax[0], wmax[1]), fmaxf(wmax[2], wmax[3]));
+                            const float VS = vmax > 0.f ? fx_vscale(vmax) : 1.f;
+                            // contributions of the batch (slot order: warps take consecutive runs of 32)
+                            for (int sl = qt; sl < cnt; sl += 128) {
+                                const int l = cellof[sl];
+                                if (l < 0) continue;
+                                const int cc[3] = {x, y, z0 - 1 + l};
+                                float f[3], lo[3], hi[3];
+                                int o0[3];
+#pragma unroll
+                                for (int d = 0; d < 3; d++) {
+                                    f[d] = stage[d * FX_PCAP + sl] * hinv3[d] - (float)cc[d];
+                                    // the two non-zero tent weights of the cell-centred nodes at
+                                    // offsets o0, o0 + 1 (o0 = -1 below the centre, 0 above)
+                                    const bool low = f[d] < 0.5f;
+                                    o0[d] = low ? -1 : 0;
+                                    lo[d] = low ? 0.5f - f[d] : 1.5f - f[d];
+                                    hi[d] = low ? 0.5f + f[d] : f[d] - 0.5f;
+                                }
+                                // row accumulator index of (dx, dy, dz) for field fld
+                                auto at = [&](int fld, int dx, int dy, int dz) {
+                                    return ((fld * 3 + dx + 1) * 3 + dy + 1) * FX_RZ + l + 1 + dz;
+                                };
+                                // density (getCellsAround + trilinear, simulator.cpp:354-368)
+#pragma unroll
+                                for (int ox = 0; ox < 2; ox++)
+#pragma unroll
+                                    for (int oy = 0; oy < 2; oy++) {
+                                        const float wxy = (ox ? hi[0] : lo[0]) * (oy ? hi[1] : lo[1]) * WS;
+#pragma unroll
+                                        for (int oz = 0; oz < 2; oz++)
+                                            atomicAdd(&racc[at(6, o0[0] + ox, o0[1] + oy, o0[2] + oz)],
+                                                      fx_round(wxy * (oz ? hi[2] : lo[2])));
+                                    }
+                                // faces of the three axes (getFacesAround + p2gTransfer, simulator.cpp:314-352)
+#pragma unroll
+                                for (int ax = 0; ax < 3; ax++) {
+                                    const int b = ax == 0 ? 1 : 0, c = ax == 2 ? 1 : 2;
+                                    const float va = stage[(3 + ax) * FX_PCAP + sl];
+                                    float K = va, ka = 0.f, kb = 0.f, kc = 0.f;
+                                    if (APIC) {
+                                        const float c0 = stage[(6 + 3 * ax) * FX_PCAP + sl];
+                                        const float c1 = stage[(7 + 3 * ax) * FX_PCAP + sl];
+                                        const float c2 = stage[(8 + 3 * ax) * FX_PCAP + sl];
+                                        const float cm[3] = {c0, c1, c2};
+                                        // v_a + c_a . (face - pos): face - pos = h (ii - f_a) along a and
+                                        // h (o + 0.5 - f) across (z scaled by zr in 2D mode)
+                                        K -= h * (cm[0] * f[0] + cm[1] * f[1] + cm[2] * f[2] * zr);
+                                        ka = h * cm[ax] * (ax == 2 ? zr : 1.f);
+                                        kb = h * cm[b] * (b == 2 ? zr : 1.f);
+                                        kc = h * cm[c] * (c == 2 ? zr : 1.f);
+                                    }
+#pragma unroll
+                                    for (int ii = 0; ii < 2; ii++) {
+                                        const float wn = (ii ? f[ax] : 1.f - f[ax]) * WS;
+#pragma unroll
+                                        for (int jb = 0; jb < 2; jb++) {
+                                            const float wnb = wn * (jb ? hi[b] : lo[b]);
+                                            const int db = o0[b] + jb;
+#pragma unroll
+                                            for (int jc = 0; jc < 2; jc++) {
+                                                const int dc = o0[c] + jc;
+                                                const float w = wnb * (jc ? hi[c] : lo[c]);  // weight x 2^21
+                                                const float val = APIC ? K + ka * (float)ii + kb * ((float)db + 0.5f) +
+                                                                             kc * ((float)dc + 0.5f)
+                                                                       : K;
+                                                int d3[3];
+                                                d3[ax] = ii - 1;
+                                                d3[b] = db;
+                                                d3[c] = dc;
+                                                const int e = at(0, d3[0], d3[1], d3[2]);
+                                                atomicAdd(&racc[e + ax * 9 * FX_RZ], fx_round(w * (val * (VS / WS))));
+                                                atomicAdd(&racc[e + (3 + ax) * 9 * FX_RZ], fx_round(w));
+                                            }
+                                        }
+                                    }
+                                }
+                            }
+                            fx_quad_bar(quad);
+                            // the batch's sums into the plane ring (owned targets), accumulator cleared
+                            const float inv_w = 1.f / WS, inv_v = 1.f / VS;
+                            for (int k = qt; k < FX_RACC; k += 128) {
+                                const int v = racc[k];
+                                if (v == 0) continue;
+                                racc[k] = 0;
+                                const int zt = k % FX_RZ, dy = (k / FX_RZ) % 3 - 1, dx = (k / (3 * FX_RZ)) % 3 - 1;
+                                const int fld = k / (9 * FX_RZ);
+                                const int px = x + dx, ty = y + dy - y0, tz = zt - 1;  // z = z0 - 2 + zt
+                                if (px < xa || px >= xe || ty < 0 || ty >= ny_left || tz < 0 || tz >= nz_left) continue;
+                                planes[((px % 3) * 7 + fld) * FX_PLANE + ty * FX_WZ + tz] +=
+                                    (float)v * (fld < 3 ? inv_v : inv_w);
+                            }
+                        }
+                    }
+                    __syncthreads();  // phase boundary
+                }
+            }
+            // plane x - 1 is complete: write it out and clear its slot for plane x + 2
+            const int xf = x - 1;
+            if (xf >= xa && xf < xe) {
+                const int slot = xf % 3;
+                for (int k = threadIdx.x; k < FX_PLANE; k += FX_THREADS) {
+                    const int ty = k / FX_WZ, tz = k % FX_WZ;
+                    float* pl = planes + slot * 7 * FX_PLANE + k;
+                    if (ty < ny_left && tz < nz_left) {
+                        const long long cell = gidx(g, xf, y0 + ty, z0 + tz);
+#pragma unroll
+                        for (int ax = 0; ax < 3; ax++) {
+                            const float w = pl[(3 + ax) * FX_PLANE];
+                            a.u[ax][cell] = (w > 1e-6f) ? pl[ax * FX_PLANE] / w : 0.f;
+                        }
+                        a.flags[cell] = (a.cstart[cell + 1] > a.cstart[cell]) ? C_WATER : C_AIR;
+                        a.avg[cell] = pl[6 * FX_PLANE];
+                    }
+#pragma unroll
+                    for (int fld = 0; fld < 7; fld++) pl[fld * FX_PLANE] = 0.f;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // the last CTA out resets the counters for the next launch
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&a.work[1], 1) == (int)gridDim.x - 1) {
+            a.work[0] = 0;
+            a.work[1] = 0;
+            __threadfence();
+        }
+    }
+}
+
 // ---- TMA / mbarrier helpers (inline PTX) ------------------------------------
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return (unsigned)__cvta_generic_to_shared(p);
@@ -491,7 +832,7 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
 
 void launch_p2g(fsim_ctx* ctx) {
     const GridGeom& g = ctx->g;
-    P2GArgs a;
+    P2GFxArgs a;
     a.p = ctx->buf[ctx->cur];
     a.perm = ctx->perm;
     a.cstart = ctx->cstart;
@@ -499,17 +840,20 @@ void launch_p2g(fsim_ctx* ctx) {
     for (int k = 0; k < 3; k++) a.u[k] = ctx->u[k];
     a.flags = ctx->flags;
     a.avg = ctx->avg;
-    a.ntx = ceil_div(g.nx, PX);
-    a.nty = ceil_div(g.ny, PY);
-    a.ntz = ceil_div(g.nz, PZ);
-    const int nb = a.ntx * a.nty * a.ntz;
+    a.work = ctx->d_misc;
+    a.nsx = ceil_div(g.nx, FX_LX);
+    a.npy = ceil_div(g.ny, FX_SY);
+    a.npz = ceil_div(g.nz, FX_SZ);
+    a.nitems = a.nsx * a.npy * a.npz;
+    const int grid = std::min(a.nitems, 2 * ctx->num_sms);
     ctx->launches += 1;
-    set_smem_limit((const void*)k_p2g<false>, P2G_SMEM);
-    set_smem_limit((const void*)k_p2g<true>, P2G_SMEM);
-    if (ctx->prm.transfer == FSIM_APIC)
-        k_p2g<true><<<nb, P2G_THREADS, P2G_SMEM, ctx->stream>>>(a);
-    else
-        k_p2g<false><<<nb, P2G_THREADS, P2G_SMEM, ctx->stream>>>(a);
+    if (ctx->prm.transfer == FSIM_APIC) {
+        set_smem_limit((const void*)k_p2g_fx<true>, fx_smem<true>());
+        k_p2g_fx<true><<<grid, FX_THREADS, fx_smem<true>(), ctx->stream>>>(a);
+    } else {
+        set_smem_limit((const void*)k_p2g_fx<false>, fx_smem<false>());
+        k_p2g_fx<false><<<grid, FX_THREADS, fx_smem<false>(), ctx->stream>>>(a);
+    }
 }
 
 // P2G on caller-provided buffers (used by the allocation-free entry point in
