@@ -238,65 +238,47 @@ __global__ void __launch_bounds__(P2G_THREADS, 2) k_p2g(const P2GArgs a) {
 //
 // The context path's P2G.  A work item is a pencil segment: FX_SY x FX_SZ
 // owned cells in (y, z) over FX_LX owned x-slices.  The CTA sweeps the
-// segment's slices in x (plus one halo slice at each end) and walks, in each
-// slice, the owned footprint and its one-cell ring (18 rows of 32 cells).
-// Contributions reach the neighbouring x-planes only, so three x-planes of
-// FP32 accumulators (7 fields over the owned footprint) live in shared memory
-// as a ring; after slice x, plane x - 1 is complete: it is normalised (v /
-// weight if weight > 1e-6, else 0; WATER where a particle is; avgPNum),
-// written out and cleared for plane x + 2.  Contributions outside the owned
-// footprint are dropped (the neighbouring pencil computes them from the same
-// ring particles): the walk is 1.2x the owned cells.
+// segment's slices in x (plus one halo slice at each end); in each slice it
+// takes the particles of the owned footprint and its one-cell ring (18 rows of
+// 32 cells, 18 contiguous runs of the cell-sorted order).  A particle's
+// contributions reach the neighbouring x-planes only, so three x-planes of
+// accumulators (7 fields: face weight and weighted velocity per axis, density,
+// over the footprint plus a two-cell margin) live in shared memory as a ring;
+// after slice x, plane x - 1 is complete: it is normalised (v / weight if the
+// weight exceeds 1e-6, else 0; WATER where a particle is; avgPNum), written
+// out and cleared for plane x + 2.  Only owned cells are written; the
+// neighbouring pencil computes the others from the same ring particles (the
+// walk is 1.2x the owned cells).
 //
-// A warp quad takes one walk row (32 cells, one contiguous run of the
-// cell-sorted order) at a time, in batches of up to FX_PCAP particles:
-//  * the quad stages the batch's particles into shared memory with coalesced
-//    loads, placing them rank-major (the first particle of every cell, then
-//    the second ...), so that the 32 lanes of a warp mostly hold particles of
-//    different cells and their atomic targets rarely meet;
-//  * every thread takes particles of the batch and adds each particle's 56
-//    contributions (8 faces x 3 axes, weight and weighted velocity, and 8
-//    density weights) to a row accumulator (3 x 3 x 34 cells around the row,
-//    7 fields) with INT32 shared-memory atomics in fixed point: weights scaled
-//    by 2^21, weighted velocities by 2^21 / 2^ceil(log2 Vmax) with Vmax the
-//    batch's largest |v_a| + h sum_b |c_ab| (the z term scaled by the 2D
-//    mode's cell aspect), so every term is below 2^21 in
-//    magnitude and a batch's sums stay below 2^29 -- no overflow, a rounding
-//    of 2^-21 of the batch's largest term, and integer sums that do not
-//    depend on the order of the atomics;
-//  * the batch's sums are converted back to FP32 and added to the plane ring
-//    with plain shared-memory adds.
-// Quad q handles walk rows 6q .. 6q + 5 in two phases of three rows (a CTA
-// barrier between phases), so rows handled at the same time are at least 5
-// apart and their plane targets (rows +-1) never meet: the plane ring gets
-// its contributions in a fixed order and P2G is reproducible bit for bit.
-// Particles with a non-finite position, velocity or C contribute nothing.
+// Every thread takes particles of the slice and adds each particle's 56
+// contributions (8 faces on each axis, weight and weighted velocity, and 8
+// density weights; getFacesAround / getCellsAround stencils) to the ring with
+// INT32 shared-memory atomics in fixed point: weights times 2^21, weighted
+// velocities times 2^21 / 2^ceil(log2 Vmax), Vmax = the step's largest |v_a|
+// (recorded by the advection pass) + h max(1, aspect) times the largest
+// sum_b |c_ab| (recorded by G2P and uploads).  Every term is then below 2^21
+// in magnitude, is rounded to 2^-21 of the largest possible term, and integer
+// sums do not depend on the order of the atomics: P2G is reproducible bit for
+// bit.  (A plane cell gathers a few hundred terms at most -- 2^31 / 2^21 = 1024
+// would be needed to overflow.)  Lanes take particles 12 apart in the sorted
+// order, so the lanes of a warp mostly hold different cells and their atomic
+// targets rarely meet.  A particle with a non-finite position, velocity or C
+// contributes nothing; one outside its bound (which the bounds exclude) sets
+// FSIM_DERR_P2G_RANGE and contributes nothing.
 //
-// Work items come from a counter (d_misc[0]); the last CTA to finish resets it
-// and the exit counter (d_misc[1]) for the next launch.
+// Work items come from a counter (d_misc[0]); the last CTA to finish resets it,
+// the exit counter (d_misc[1]) and the velocity bound (d_misc[2]).
 constexpr int FX_SY = 16;             // owned y cells per pencil
 constexpr int FX_WZ = 32;             // walk cells per row
 constexpr int FX_SZ = FX_WZ - 2;      // owned z cells per pencil
 constexpr int FX_WY = FX_SY + 2;      // walk rows per slice
 constexpr int FX_LX = 32;             // owned x slices per work item
-constexpr int FX_QUADS = 3;
-constexpr int FX_THREADS = FX_QUADS * 128;
-constexpr int FX_PCAP = 192;          // particles per batch
-constexpr int FX_PLANE = FX_SY * FX_WZ;
-constexpr int FX_RZ = FX_WZ + 2;      // row accumulator z extent (z0 - 2 .. z0 + 31)
-constexpr int FX_RACC = 7 * 9 * FX_RZ;  // row accumulator entries (field, dx, dy, z)
-static_assert(FX_WY == 6 * FX_QUADS, "each quad takes six walk rows");
-
-template <bool APIC>
-__host__ __device__ constexpr int fx_fields() { return APIC ? 15 : 6; }
-// per-quad scratch (floats / ints): staged fields, cell of each staged slot,
-// rank tables, cell starts, warp maxima, row accumulator
-template <bool APIC>
-__host__ __device__ constexpr int fx_quad_words() {
-    return fx_fields<APIC>() * FX_PCAP + FX_PCAP + 2 * (FX_PCAP + 1) + 36 + 4 + FX_RACC;
-}
-template <bool APIC>
-constexpr int fx_smem() { return (3 * 7 * FX_PLANE + FX_QUADS * fx_quad_words<APIC>()) * 4; }
+constexpr int FX_THREADS = 384;
+constexpr int FX_WARPS = FX_THREADS / 32;
+constexpr int FX_PY = FX_SY + 4;      // plane rows: y0 - 2 .. y0 + SY + 1
+constexpr int FX_PZ = FX_SZ + 4;      // plane columns: z0 - 2 .. z0 + SZ + 1
+constexpr int FX_PLANE = FX_PY * FX_PZ;
+constexpr int FX_SMEM = 3 * 7 * FX_PLANE * 4;
 
 struct P2GFxArgs {
     ParticleBuf p;
@@ -306,49 +288,38 @@ struct P2GFxArgs {
     float* u[3];
     uint8_t* flags;
     float* avg;
-    int* work;          // [0] next item, [1] CTAs done
+    int* misc;          // [0] next item, [1] CTAs done, [2] |v| bound, [3] C bound (FP32 bits)
+    unsigned* err;
     int nsx, npy, npz;  // segments in x, pencils in y and z
     int nitems;
 };
 
-__device__ __forceinline__ void fx_quad_bar(int quad) {
-    asm volatile("bar.sync %0, 128;" ::"r"(quad + 1) : "memory");
-}
-
-// round(x) for |x| < 2^22: adding 1.5 * 2^23 leaves the integer in the low
-// mantissa bits
+// round(x) for |x| < 2^22: adding 1.5 * 2^23 leaves the integer in the low mantissa bits
 __device__ __forceinline__ int fx_round(float x) { return __float_as_int(x + 12582912.0f) - 0x4B400000; }
-
-// 2^(21 - e) with 2^e the smallest power of two above vmax (vmax > 0, finite)
-__device__ __forceinline__ float fx_vscale(float vmax) {
-    int e;
-    frexpf(vmax, &e);  // vmax = m 2^e, 0.5 <= m < 1
-    return ldexpf(1.f, 21 - e);
-}
 
 template <bool APIC>
 __global__ void __launch_bounds__(FX_THREADS, 2) k_p2g_fx(const P2GFxArgs a) {
-    extern __shared__ float sm[];
-    constexpr int NF = fx_fields<APIC>();
-    float* planes = sm;                                        // [3 slots][7 fields][FX_PLANE]
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int quad = warp >> 2, qw = warp & 3, qt = threadIdx.x & 127;
-    float* qbase = sm + 3 * 7 * FX_PLANE + quad * fx_quad_words<APIC>();
-    float* stage = qbase;                                      // [NF][FX_PCAP]
-    int* cellof = reinterpret_cast<int*>(stage + NF * FX_PCAP);  // [FX_PCAP] walk cell of a slot, -1 invalid
-    int* rank_off = cellof + FX_PCAP;                          // [FX_PCAP + 1] slots before rank r
-    unsigned* rank_mask = reinterpret_cast<unsigned*>(rank_off + FX_PCAP + 1);  // cells holding rank r
-    int* cs = reinterpret_cast<int*>(rank_mask + FX_PCAP + 1); // [33] batch-relative cell starts (+3 pad)
-    float* wmax = reinterpret_cast<float*>(cs + 36);           // [4] per-warp Vmax
-    int* racc = reinterpret_cast<int*>(wmax + 4);              // [7][3][3][FX_RZ]
+    extern __shared__ int ring[];  // [3 slots][7 fields][FX_PLANE]
     __shared__ int s_item;
+    __shared__ int s_pre[FX_WY + 1], s_beg[FX_WY];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const GridGeom& g = a.g;
     const float h = g.h, zr = g.two_d ? (float)(g.hzd * g.hinvd) : 1.f;
-    const float hinv3[3] = {g.hinv, g.hinv, g.hzinv};
+    // the fixed-point scales, the same for every CTA of the launch
     const float WS = 2097152.f;  // 2^21
+    float vmax = __uint_as_float((unsigned)a.misc[2]);
+    if (APIC) vmax += h * fmaxf(1.f, zr) * __uint_as_float((unsigned)a.misc[3]);
+    vmax *= 1.001f;  // FP32 rounding of the terms
+    float VS = 1.f;
+    if (vmax > 0.f) {
+        int e;
+        frexpf(vmax, &e);  // vmax = m 2^e, 0.5 <= m < 1
+        VS = ldexpf(1.f, 21 - e);
+    }
+    const float vsw = VS / WS;
 
     for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(&a.work[0], 1);
+        if (threadIdx.x == 0) s_item = atomicAdd(&a.misc[0], 1);
         __syncthreads();
         const int item = s_item;
         if (item >= a.nitems) break;
@@ -356,220 +327,169 @@ __global__ void __launch_bounds__(FX_THREADS, 2) k_p2g_fx(const P2GFxArgs a) {
         const int xa = sxi * FX_LX, xe = min(xa + FX_LX, g.nx);
         const int y0 = pyi * FX_SY, z0 = pzi * FX_SZ;
         const int ny_left = min(FX_SY, g.ny - y0), nz_left = min(FX_SZ, g.nz - z0);
-        for (int k = threadIdx.x; k < 3 * 7 * FX_PLANE; k += FX_THREADS) planes[k] = 0.f;
-        for (int k = qt; k < FX_RACC; k += 128) racc[k] = 0;
-        __syncthreads();
+        const int zlo = max(z0 - 1, 0), zhi = min(z0 - 1 + FX_WZ, g.nz);
+        for (int k = threadIdx.x; k < 3 * 7 * FX_PLANE; k += FX_THREADS) ring[k] = 0;
         for (int x = xa - 1; x <= xe; x++) {
             if (x >= 0 && x < g.nx) {
-                for (int phase = 0; phase < 2; phase++) {
-                    for (int rr = 0; rr < 3; rr++) {
-                        const int wy = quad * 6 + phase * 3 + rr;
-                        const int y = y0 - 1 + wy;
-                        if (y < 0 || y >= g.ny) continue;  // uniform across the quad
+                // the slice's 18 walk rows as one list of sorted particles
+                if (warp == 0) {
+                    const int y = y0 - 1 + lane;
+                    int beg = 0, len = 0;
+                    if (lane < FX_WY && y >= 0 && y < g.ny) {
                         const long long rowc = gidx(g, x, y, 0);
-                        const int zlo = max(z0 - 1, 0), zhi = min(z0 - 1 + FX_WZ, g.nz);
-                        const int rb = a.cstart[rowc + zlo], re = a.cstart[rowc + zhi];
-                        for (int bs = rb; bs < re; bs += FX_PCAP) {
-                            const int cnt = min(FX_PCAP, re - bs);
-                            // batch-relative cell starts of the 32 walk cells and the rank tables
-                            if (qw == 0) {
-                                const int z = z0 - 1 + lane;
-                                int c0 = 0, c1 = 0;
-                                if (z >= 0 && z < g.nz) {
-                                    c0 = min(max(a.cstart[rowc + z] - bs, 0), cnt);
-                                    c1 = min(max(a.cstart[rowc + z + 1] - bs, 0), cnt);
-                                } else {
-                                    c0 = c1 = z < 0 ? 0 : cnt;
+                        beg = a.cstart[rowc + zlo];
+                        len = a.cstart[rowc + zhi] - beg;
+                    }
+                    int incl = len;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= o) incl += t;
+                    }
+                    if (lane < FX_WY) {
+                        s_beg[lane] = beg;
+                        s_pre[lane + 1] = incl;
+                    }
+                    if (lane == 0) s_pre[0] = 0;
+                }
+                __syncthreads();
+                const int total = s_pre[FX_WY];
+                const int slot_base[3] = {((x + 2) % 3) * 7 * FX_PLANE, ((x + 3) % 3) * 7 * FX_PLANE,
+                                          ((x + 4) % 3) * 7 * FX_PLANE};  // planes x - 1, x, x + 1
+                for (int base = 0; base < total; base += FX_THREADS) {
+                    const int j = base + lane * FX_WARPS + warp;  // lanes 12 particles apart
+                    if (j >= total) continue;
+                    int lo = 0, hi = FX_WY;  // the row r with s_pre[r] <= j < s_pre[r + 1]
+#pragma unroll
+                    for (int step = 0; step < 5; step++) {
+                        const int mid = (lo + hi) >> 1;
+                        if (mid < FX_WY && s_pre[mid] <= j) lo = mid;
+                        else hi = mid;
+                    }
+                    const int r = lo;
+                    const uint32_t i = a.perm[s_beg[r] + (j - s_pre[r])];
+                    const float px = a.p.p[0][i], py = a.p.p[1][i], pz = a.p.p[2][i];
+                    float v[3], cm[9];
+#pragma unroll
+                    for (int d = 0; d < 3; d++) v[d] = a.p.v[d][i];
+                    if (APIC) {
+#pragma unroll
+                        for (int k = 0; k < 9; k++) cm[k] = a.p.c[k][i];
+                    }
+                    // this particle's bound (and finiteness)
+                    float pm = 0.f;
+                    bool ok = isfinite(px) && isfinite(py) && isfinite(pz);
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        float m = fabsf(v[d]);
+                        if (APIC) m += h * (fabsf(cm[3 * d]) + fabsf(cm[3 * d + 1]) + fabsf(cm[3 * d + 2]) * zr);
+                        pm = fmaxf(pm, m);
+                    }
+                    ok &= isfinite(pm);
+                    if (!ok) continue;
+                    if (pm * VS >= WS) {
+                        atomicOr(a.err, FSIM_DERR_P2G_RANGE);
+                        continue;
+                    }
+                    const int cy = y0 - 1 + r;
+                    const int cz = min(max((int)(pz * g.hzinv), 0), g.nz - 1);  // the sort key's z
+                    const float f[3] = {px * g.hinv - (float)x, py * g.hinv - (float)cy, pz * g.hzinv - (float)cz};
+                    float lo3[3], hi3[3];
+                    int o0[3];
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        // the two non-zero tent weights of the cell-centred nodes at o0, o0 + 1
+                        const bool low = f[d] < 0.5f;
+                        o0[d] = low ? -1 : 0;
+                        lo3[d] = low ? 0.5f - f[d] : 1.5f - f[d];
+                        hi3[d] = low ? 0.5f + f[d] : f[d] - 0.5f;
+                    }
+                    // ring index of cell offset (dx, dy, dz) without the field: slot + row + column
+                    const int cell0 = (cy - y0 + 2) * FX_PZ + (cz - z0 + 2);
+                    // density (getCellsAround + trilinear, simulator.cpp:354-368)
+#pragma unroll
+                    for (int ox = 0; ox < 2; ox++)
+#pragma unroll
+                        for (int oy = 0; oy < 2; oy++) {
+                            const float wxy = (ox ? hi3[0] : lo3[0]) * (oy ? hi3[1] : lo3[1]) * WS;
+                            const int e0 = slot_base[o0[0] + ox + 1] + 6 * FX_PLANE + cell0 + (o0[1] + oy) * FX_PZ + o0[2];
+#pragma unroll
+                            for (int oz = 0; oz < 2; oz++) atomicAdd(&ring[e0 + oz], fx_round(wxy * (oz ? hi3[2] : lo3[2])));
+                        }
+                    // faces of the three axes (getFacesAround + p2gTransfer, simulator.cpp:314-352)
+#pragma unroll
+                    for (int ax = 0; ax < 3; ax++) {
+                        const int b = ax == 0 ? 1 : 0, c = ax == 2 ? 1 : 2;
+                        // v_a + c_a . (face - pos): face - pos = h (ii - f_a) along a and
+                        // h (o + 0.5 - f) across (z terms scaled by zr in 2D mode)
+                        float K = v[ax], ka = 0.f, kb = 0.f, kc = 0.f;
+                        if (APIC) {
+                            const float* ca = cm + 3 * ax;
+                            K -= h * (ca[0] * f[0] + ca[1] * f[1] + ca[2] * f[2] * zr);
+                            ka = h * ca[ax] * (ax == 2 ? zr : 1.f);
+                            kb = h * ca[b];
+                            kc = h * ca[c] * (c == 2 ? zr : 1.f);
+                            K += kb * ((float)o0[b] + 0.5f) + kc * ((float)o0[c] + 0.5f);
+                        }
+                        const int strideb = b == 0 ? 0 : (b == 1 ? FX_PZ : 1);
+                        const int stridec = c == 1 ? FX_PZ : 1;
+                        // offsets of the stencil's base corner: normal -1, transverse o0
+                        const int ob_x = ax == 0 ? -1 : o0[0];
+                        const int e0 = cell0 + (ax == 1 ? -1 : o0[1]) * FX_PZ + (ax == 2 ? -1 : o0[2]);
+#pragma unroll
+                        for (int ii = 0; ii < 2; ii++) {
+                            const float wn = (ii ? f[ax] : 1.f - f[ax]) * WS;
+#pragma unroll
+                            for (int jb = 0; jb < 2; jb++) {
+                                const float wnb = wn * (jb ? hi3[b] : lo3[b]);
+#pragma unroll
+                                for (int jc = 0; jc < 2; jc++) {
+                                    const float w = wnb * (jc ? hi3[c] : lo3[c]);  // weight x 2^21
+                                    const float val = K + ka * (float)ii + kb * (float)jb + kc * (float)jc;
+                                    // slot (x offset) and in-plane offset of this corner
+                                    const int dxo = ob_x + (ax == 0 ? ii : (b == 0 ? jb : 0));
+                                    const int e = slot_base[dxo + 1] + e0 + (ax == 0 ? 0 : ii * (ax == 1 ? FX_PZ : 1)) +
+                                                  jb * strideb + jc * stridec;
+                                    atomicAdd(&ring[e + ax * FX_PLANE], fx_round(w * (val * vsw)));
+                                    atomicAdd(&ring[e + (3 + ax) * FX_PLANE], fx_round(w));
                                 }
-                                cs[lane] = c0;
-                                if (lane == 31) cs[32] = cnt;
-                                const int c = c1 - c0;
-                                int maxc = c;
-#pragma unroll
-                                for (int o = 16; o > 0; o >>= 1) maxc = max(maxc, __shfl_xor_sync(0xffffffffu, maxc, o));
-                                int run = 0;
-                                for (int r = 0; r < maxc; r++) {
-                                    const unsigned m = __ballot_sync(0xffffffffu, c > r);
-                                    if (lane == 0) {
-                                        rank_mask[r] = m;
-                                        rank_off[r] = run;
-                                    }
-                                    run += __popc(m);
-                                }
-                            }
-                            fx_quad_bar(quad);
-                            // stage rank-major, with the batch's velocity bound
-                            float vm = 0.f;
-                            for (int j = qt; j < cnt; j += 128) {
-                                int lo = 0, hi = 32;  // the cell l with cs[l] <= j < cs[l + 1]
-#pragma unroll
-                                for (int step = 0; step < 5; step++) {
-                                    const int mid = (lo + hi) >> 1;
-                                    if (cs[mid] <= j) lo = mid;
-                                    else hi = mid;
-                                }
-                                const int l = lo;
-                                const int r = j - cs[l];
-                                const int slot = rank_off[r] + __popc(rank_mask[r] & ((1u << l) - 1u));
-                                const uint32_t i = a.perm[bs + j];
-                                float q[NF];
-#pragma unroll
-                                for (int d = 0; d < 3; d++) {
-                                    q[d] = a.p.p[d][i];
-                                    q[3 + d] = a.p.v[d][i];
-                                }
-                                if (APIC) {
-#pragma unroll
-                                    for (int k = 0; k < 9; k++) q[6 + k] = a.p.c[k][i];
-                                }
-                                bool ok = true;
-                                float pm = 0.f;
-#pragma unroll
-                                for (int d = 0; d < 3; d++) {
-                                    float m = fabsf(q[3 + d]);
-                                    // |c_d . (face - pos)| <= h sum_b |c_db| (z scaled by zr in 2D mode)
-                                    if (APIC)
-                                        m += h * (fabsf(q[6 + 3 * d]) + fabsf(q[7 + 3 * d]) + fabsf(q[8 + 3 * d]) * zr);
-                                    pm = fmaxf(pm, m);
-                                }
-#pragma unroll
-                                for (int k = 0; k < NF; k++) ok &= isfinite(q[k]);
-                                if (ok) vm = fmaxf(vm, pm);
-#pragma unroll
-                                for (int k = 0; k < NF; k++) stage[k * FX_PCAP + slot] = q[k];
-                                cellof[slot] = ok ? l : -1;
-                            }
-#pragma unroll
-                            for (int o = 16; o > 0; o >>= 1) vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, o));
-                            if (lane == 0) wmax[qw] = vm;
-                            fx_quad_bar(quad);
-                            const float vmax = fmaxf(fmaxf(wmax[0], wmax[1]), fmaxf(wmax[2], wmax[3]));
-                            const float VS = vmax > 0.f ? fx_vscale(vmax) : 1.f;
-                            // contributions of the batch (slot order: warps take consecutive runs of 32)
-                            for (int sl = qt; sl < cnt; sl += 128) {
-                                const int l = cellof[sl];
-                                if (l < 0) continue;
-                                const int cc[3] = {x, y, z0 - 1 + l};
-                                float f[3], lo[3], hi[3];
-                                int o0[3];
-#pragma unroll
-                                for (int d = 0; d < 3; d++) {
-                                    f[d] = stage[d * FX_PCAP + sl] * hinv3[d] - (float)cc[d];
-                                    // the two non-zero tent weights of the cell-centred nodes at
-                                    // offsets o0, o0 + 1 (o0 = -1 below the centre, 0 above)
-                                    const bool low = f[d] < 0.5f;
-                                    o0[d] = low ? -1 : 0;
-                                    lo[d] = low ? 0.5f - f[d] : 1.5f - f[d];
-                                    hi[d] = low ? 0.5f + f[d] : f[d] - 0.5f;
-                                }
-                                // row accumulator index of (dx, dy, dz) for field fld
-                                auto at = [&](int fld, int dx, int dy, int dz) {
-                                    return ((fld * 3 + dx + 1) * 3 + dy + 1) * FX_RZ + l + 1 + dz;
-                                };
-                                // density (getCellsAround + trilinear, simulator.cpp:354-368)
-#pragma unroll
-                                for (int ox = 0; ox < 2; ox++)
-#pragma unroll
-                                    for (int oy = 0; oy < 2; oy++) {
-                                        const float wxy = (ox ? hi[0] : lo[0]) * (oy ? hi[1] : lo[1]) * WS;
-#pragma unroll
-                                        for (int oz = 0; oz < 2; oz++)
-                                            atomicAdd(&racc[at(6, o0[0] + ox, o0[1] + oy, o0[2] + oz)],
-                                                      fx_round(wxy * (oz ? hi[2] : lo[2])));
-                                    }
-                                // faces of the three axes (getFacesAround + p2gTransfer, simulator.cpp:314-352)
-#pragma unroll
-                                for (int ax = 0; ax < 3; ax++) {
-                                    const int b = ax == 0 ? 1 : 0, c = ax == 2 ? 1 : 2;
-                                    const float va = stage[(3 + ax) * FX_PCAP + sl];
-                                    float K = va, ka = 0.f, kb = 0.f, kc = 0.f;
-                                    if (APIC) {
-                                        const float c0 = stage[(6 + 3 * ax) * FX_PCAP + sl];
-                                        const float c1 = stage[(7 + 3 * ax) * FX_PCAP + sl];
-                                        const float c2 = stage[(8 + 3 * ax) * FX_PCAP + sl];
-                                        const float cm[3] = {c0, c1, c2};
-                                        // v_a + c_a . (face - pos): face - pos = h (ii - f_a) along a and
-                                        // h (o + 0.5 - f) across (z scaled by zr in 2D mode)
-                                        K -= h * (cm[0] * f[0] + cm[1] * f[1] + cm[2] * f[2] * zr);
-                                        ka = h * cm[ax] * (ax == 2 ? zr : 1.f);
-                                        kb = h * cm[b] * (b == 2 ? zr : 1.f);
-                                        kc = h * cm[c] * (c == 2 ? zr : 1.f);
-                                    }
-#pragma unroll
-                                    for (int ii = 0; ii < 2; ii++) {
-                                        const float wn = (ii ? f[ax] : 1.f - f[ax]) * WS;
-#pragma unroll
-                                        for (int jb = 0; jb < 2; jb++) {
-                                            const float wnb = wn * (jb ? hi[b] : lo[b]);
-                                            const int db = o0[b] + jb;
-#pragma unroll
-                                            for (int jc = 0; jc < 2; jc++) {
-                                                const int dc = o0[c] + jc;
-                                                const float w = wnb * (jc ? hi[c] : lo[c]);  // weight x 2^21
-                                                const float val = APIC ? K + ka * (float)ii + kb * ((float)db + 0.5f) +
-                                                                             kc * ((float)dc + 0.5f)
-                                                                       : K;
-                                                int d3[3];
-                                                d3[ax] = ii - 1;
-                                                d3[b] = db;
-                                                d3[c] = dc;
-                                                const int e = at(0, d3[0], d3[1], d3[2]);
-                                                atomicAdd(&racc[e + ax * 9 * FX_RZ], fx_round(w * (val * (VS / WS))));
-                                                atomicAdd(&racc[e + (3 + ax) * 9 * FX_RZ], fx_round(w));
-                                            }
-                                        }
-                                    }
-                                }
-                            }
-                            fx_quad_bar(quad);
-                            // the batch's sums into the plane ring (owned targets), accumulator cleared
-                            const float inv_w = 1.f / WS, inv_v = 1.f / VS;
-                            for (int k = qt; k < FX_RACC; k += 128) {
-                                const int v = racc[k];
-                                if (v == 0) continue;
-                                racc[k] = 0;
-                                const int zt = k % FX_RZ, dy = (k / FX_RZ) % 3 - 1, dx = (k / (3 * FX_RZ)) % 3 - 1;
-                                const int fld = k / (9 * FX_RZ);
-                                const int px = x + dx, ty = y + dy - y0, tz = zt - 1;  // z = z0 - 2 + zt
-                                if (px < xa || px >= xe || ty < 0 || ty >= ny_left || tz < 0 || tz >= nz_left) continue;
-                                planes[((px % 3) * 7 + fld) * FX_PLANE + ty * FX_WZ + tz] +=
-                                    (float)v * (fld < 3 ? inv_v : inv_w);
                             }
                         }
                     }
-                    __syncthreads();  // phase boundary
                 }
+                __syncthreads();
             }
-            // plane x - 1 is complete: write it out and clear its slot for plane x + 2
+            // plane x - 1 is complete: write its owned cells out and clear its slot for plane x + 2
             const int xf = x - 1;
+            int* pl = ring + ((xf + 3) % 3) * 7 * FX_PLANE;
             if (xf >= xa && xf < xe) {
-                const int slot = xf % 3;
-                for (int k = threadIdx.x; k < FX_PLANE; k += FX_THREADS) {
-                    const int ty = k / FX_WZ, tz = k % FX_WZ;
-                    float* pl = planes + slot * 7 * FX_PLANE + k;
-                    if (ty < ny_left && tz < nz_left) {
-                        const long long cell = gidx(g, xf, y0 + ty, z0 + tz);
+                const float inv_w = 1.f / WS, inv_v = 1.f / VS;
+                for (int k = threadIdx.x; k < FX_SY * FX_SZ; k += FX_THREADS) {
+                    const int ty = k / FX_SZ, tz = k - ty * FX_SZ;
+                    if (ty >= ny_left || tz >= nz_left) continue;
+                    const int pc = (ty + 2) * FX_PZ + tz + 2;
+                    const long long cell = gidx(g, xf, y0 + ty, z0 + tz);
 #pragma unroll
-                        for (int ax = 0; ax < 3; ax++) {
-                            const float w = pl[(3 + ax) * FX_PLANE];
-                            a.u[ax][cell] = (w > 1e-6f) ? pl[ax * FX_PLANE] / w : 0.f;
-                        }
-                        a.flags[cell] = (a.cstart[cell + 1] > a.cstart[cell]) ? C_WATER : C_AIR;
-                        a.avg[cell] = pl[6 * FX_PLANE];
+                    for (int ax = 0; ax < 3; ax++) {
+                        const float w = (float)pl[(3 + ax) * FX_PLANE + pc] * inv_w;
+                        a.u[ax][cell] = (w > 1e-6f) ? (float)pl[ax * FX_PLANE + pc] * inv_v / w : 0.f;
                     }
-#pragma unroll
-                    for (int fld = 0; fld < 7; fld++) pl[fld * FX_PLANE] = 0.f;
+                    a.flags[cell] = (a.cstart[cell + 1] > a.cstart[cell]) ? C_WATER : C_AIR;
+                    a.avg[cell] = (float)pl[6 * FX_PLANE + pc] * inv_w;
                 }
+                __syncthreads();
             }
+            for (int k = threadIdx.x; k < 7 * FX_PLANE; k += FX_THREADS) pl[k] = 0;
             __syncthreads();
         }
     }
-    // the last CTA out resets the counters for the next launch
+    // the last CTA out resets the counters and the velocity bound for the next launch
     if (threadIdx.x == 0) {
         __threadfence();
-        if (atomicAdd(&a.work[1], 1) == (int)gridDim.x - 1) {
-            a.work[0] = 0;
-            a.work[1] = 0;
+        if (atomicAdd(&a.misc[1], 1) == (int)gridDim.x - 1) {
+            a.misc[0] = 0;
+            a.misc[1] = 0;
+            a.misc[2] = 0;
             __threadfence();
         }
     }
@@ -616,6 +536,7 @@ struct G2PArgs {
     int ids;
     int move_c;        // PIC/FLIP: carry C along the permutation
     unsigned* err;
+    unsigned* cmax;    // APIC: largest sum_b |c_ab| of the new C (FP32 bits, atomicMax; cleared before)
 };
 
 // MODE: 0 PIC, 1 FLIP, 2 APIC
@@ -719,6 +640,7 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
         }
     }
     const float hinv = a.g.hinv, hzinv = a.g.hzinv;
+    float cm_thread = 0.f;  // APIC: this thread's largest sum_b |c_ab|
     for (int j = threadIdx.x; j < total; j += blockDim.x) {
         const int k = kn;
         const uint32_t i = in;
@@ -820,11 +742,20 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
         if (MODE == 2) {
 #pragma unroll
             for (int q = 0; q < 9; q++) a.dst.c[q][k] = cnew[q];
+#pragma unroll
+            for (int r = 0; r < 3; r++) {
+                const float m = fabsf(cnew[3 * r]) + fabsf(cnew[3 * r + 1]) + fabsf(cnew[3 * r + 2]);
+                if (isfinite(m)) cm_thread = fmaxf(cm_thread, m);
+            }
         } else if (a.move_c) {
 #pragma unroll
             for (int q = 0; q < 9; q++) a.dst.c[q][k] = a.src.c[q][i];
         }
         if (a.ids) a.dst.id[k] = a.src.id[i];
+    }
+    if (MODE == 2) {
+        const unsigned mb = __reduce_max_sync(0xffffffffu, __float_as_uint(cm_thread));
+        if ((threadIdx.x & 31) == 0 && mb) atomicMax(a.cmax, mb);
     }
 }
 
@@ -840,7 +771,8 @@ void launch_p2g(fsim_ctx* ctx) {
     for (int k = 0; k < 3; k++) a.u[k] = ctx->u[k];
     a.flags = ctx->flags;
     a.avg = ctx->avg;
-    a.work = ctx->d_misc;
+    a.misc = ctx->d_misc;
+    a.err = ctx->d_err;
     a.nsx = ceil_div(g.nx, FX_LX);
     a.npy = ceil_div(g.ny, FX_SY);
     a.npz = ceil_div(g.nz, FX_SZ);
@@ -848,11 +780,11 @@ void launch_p2g(fsim_ctx* ctx) {
     const int grid = std::min(a.nitems, 2 * ctx->num_sms);
     ctx->launches += 1;
     if (ctx->prm.transfer == FSIM_APIC) {
-        set_smem_limit((const void*)k_p2g_fx<true>, fx_smem<true>());
-        k_p2g_fx<true><<<grid, FX_THREADS, fx_smem<true>(), ctx->stream>>>(a);
+        set_smem_limit((const void*)k_p2g_fx<true>, FX_SMEM);
+        k_p2g_fx<true><<<grid, FX_THREADS, FX_SMEM, ctx->stream>>>(a);
     } else {
-        set_smem_limit((const void*)k_p2g_fx<false>, fx_smem<false>());
-        k_p2g_fx<false><<<grid, FX_THREADS, fx_smem<false>(), ctx->stream>>>(a);
+        set_smem_limit((const void*)k_p2g_fx<false>, FX_SMEM);
+        k_p2g_fx<false><<<grid, FX_THREADS, FX_SMEM, ctx->stream>>>(a);
     }
 }
 
@@ -927,6 +859,8 @@ int launch_g2p(fsim_ctx* ctx) {
     a.ids = ctx->prm.track_ids ? 1 : 0;
     a.move_c = 1;
     a.err = ctx->d_err;
+    a.cmax = reinterpret_cast<unsigned*>(ctx->d_misc + MISC_CMAX);
+    if (ctx->prm.transfer == FSIM_APIC) cudaMemsetAsync(a.cmax, 0, sizeof(unsigned), ctx->stream);
     const int nb = a.ntx * a.nty * a.ntz;
     const int mode = ctx->prm.transfer;
     ctx->launches += 1;
