@@ -19,31 +19,19 @@
 namespace {
 
 // ---- AoS <-> SoA ------------------------------------------------------------
-// also raises cmax (FP32 bits) to the largest sum_b |c_ab| of the uploaded C
 __global__ void k_aos_to_soa(const float* pos, const float* vel, const float* c, long long n, ParticleBuf d,
-                             long long first, uint32_t id0, int ids, unsigned* cmax) {
+                             long long first, uint32_t id0, int ids) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    float m = 0.f;
-    if (i < n) {
-        const long long j = first + i;
+    if (i >= n) return;
+    const long long j = first + i;
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            d.p[a][j] = pos[3 * i + a];
-            d.v[a][j] = vel ? vel[3 * i + a] : 0.f;
-        }
-#pragma unroll
-        for (int a = 0; a < 9; a++) d.c[a][j] = c ? c[9 * i + a] : 0.f;
-        if (ids) d.id[j] = id0 + (uint32_t)i;
-        if (c) {
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                const float r = fabsf(c[9 * i + 3 * a]) + fabsf(c[9 * i + 3 * a + 1]) + fabsf(c[9 * i + 3 * a + 2]);
-                if (isfinite(r)) m = fmaxf(m, r);
-            }
-        }
+    for (int a = 0; a < 3; a++) {
+        d.p[a][j] = pos[3 * i + a];
+        d.v[a][j] = vel ? vel[3 * i + a] : 0.f;
     }
-    const unsigned mb = __reduce_max_sync(0xffffffffu, __float_as_uint(m));
-    if ((threadIdx.x & 31) == 0 && mb) atomicMax(cmax, mb);
+#pragma unroll
+    for (int a = 0; a < 9; a++) d.c[a][j] = c ? c[9 * i + a] : 0.f;
+    if (ids) d.id[j] = id0 + (uint32_t)i;
 }
 
 __global__ void k_soa_to_aos(ParticleBuf s, long long n, const int* dst_index, float* pos, float* vel, float* c) {
@@ -213,7 +201,6 @@ void fill_advect_args(fsim_ctx* ctx, AdvectArgs& a, double dt) {
     a.key = ctx->key;
     a.rank = ctx->rank;
     a.count = ctx->count;
-    a.vmax = reinterpret_cast<unsigned*>(ctx->d_misc + MISC_VMAX);
 }
 
 // counting sort by cell of the current buffer (keys from do_key)
@@ -375,10 +362,6 @@ int check_device_error(fsim_ctx* ctx) {
     if (e & FSIM_DERR_TMA_TIMEOUT) {
         cudaMemset(ctx->d_err, 0, sizeof(unsigned));
         return set_error(ctx, FSIM_E_TIMEOUT, "G2P tile load wait timed out");
-    }
-    if (e & FSIM_DERR_P2G_RANGE) {
-        cudaMemset(ctx->d_err, 0, sizeof(unsigned));
-        return set_error(ctx, FSIM_E_STATE, "P2G: a particle exceeded the velocity bound of its fixed-point scale");
     }
     return FSIM_OK;
 }
@@ -587,8 +570,7 @@ static int upload_particles(fsim_ctx* ctx, const float* pos, const float* vel, c
         }
     }
     k_aos_to_soa<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(dp, dv, dc, n, ctx->buf[ctx->cur], first,
-                                                            ctx->next_id, ctx->prm.track_ids ? 1 : 0,
-                                                            reinterpret_cast<unsigned*>(ctx->d_misc + MISC_CMAX));
+                                                            ctx->next_id, ctx->prm.track_ids ? 1 : 0);
     CHECK_LAUNCH(ctx);
     if (tmp) FSIM_CUDA_TRY(ctx, cudaFreeAsync(tmp, ctx->stream));
     ctx->next_id += (uint32_t)n;
@@ -602,8 +584,6 @@ int fsim_set_particles(fsim_ctx* ctx, const float* pos, const float* vel, const 
     if (rc) return rc;
     ctx->n = 0;
     ctx->next_id = 0;
-    // the new particles replace every APIC matrix: their bound starts over
-    FSIM_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_misc + MISC_CMAX, 0, sizeof(int), ctx->stream));
     rc = upload_particles(ctx, pos, vel, c, n, where, 0);
     if (rc) return rc;
     ctx->n = n;

@@ -38,7 +38,6 @@ inline cudaError_t set_smem_limit(const void* kern, int bytes) {
 // Device error flags (OR-ed into ctx->d_err, read by the host after a step).
 #define FSIM_DERR_TMA_TIMEOUT 1u
 #define FSIM_DERR_NAN 2u
-#define FSIM_DERR_P2G_RANGE 4u  // a P2G term exceeded the fixed-point range of its velocity bound
 
 // Geometry of the padded grid.  Cells (x, y, z) with 0 <= z < nz are the
 // reference's cells; storage pads z to pz (a multiple of 4 so every row starts

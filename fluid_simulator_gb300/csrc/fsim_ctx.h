@@ -163,14 +163,8 @@ struct AdvectArgs {
     uint32_t* key;
     uint32_t* rank;
     int* count;
-    unsigned* vmax;        // max |v_a| of the keyed particles (FP32 bits, atomicMax), or null
 };
 void launch_advect(const AdvectArgs& a, cudaStream_t s);
-// Device words in ctx->d_misc: [0..1] the P2G work counters, [2] the largest
-// |v_a| of the particles keyed since the last P2G (FP32 bits; advect raises
-// it, P2G reads and clears it), [3] the largest sum_b |c_ab| over a of the
-// particles' APIC matrices (FP32 bits; raised by uploads, rebuilt by G2P).
-enum { MISC_P2G_WORK = 0, MISC_VMAX = 2, MISC_CMAX = 3 };
 void launch_scan(const int* in, int* out, long long n, int* block_sums, cudaStream_t s);
 // perm[cstart[key] + rank] = index, then each cell's segment in ascending
 // particle index (two kernels when n > 0)

@@ -213,17 +213,6 @@ __global__ void __launch_bounds__(256) k_advect(const AdvectArgs a) {
         }
     }
     if (!a.do_key) return;
-    if (a.vmax) {
-        // the largest velocity component the next P2G will see (its fixed-point scale)
-        float m = 0.f;
-        if (live && key != FSIM_DEAD_KEY) {
-            const float vx = a.p.v[0][i], vy = a.p.v[1][i], vz = a.p.v[2][i];
-            const float mv = fmaxf(fabsf(vx), fmaxf(fabsf(vy), fabsf(vz)));
-            if (isfinite(mv)) m = mv;
-        }
-        const unsigned mb = __reduce_max_sync(0xffffffffu, __float_as_uint(m));
-        if ((threadIdx.x & 31) == 0 && mb) atomicMax(a.vmax, mb);
-    }
     // warp-aggregated cell counting: one atomic per distinct key per warp
     const unsigned peers = __match_any_sync(0xffffffffu, key);
     const int lane = threadIdx.x & 31;

@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(P2G_THREADS, 2) k_p2g(const P2GArgs a) {
     }
 }
 
-// ---- P2G: x sweep over pencils, particle-parallel fixed-point accumulation ----
+// ---- P2G: x sweep over pencils, particle-parallel shared-memory accumulation ----
 //
 // The context path's P2G.  A work item is a pencil segment: FX_SY x FX_SZ
 // owned cells in (y, z) over FX_LX owned x-slices.  The CTA sweeps the
@@ -242,32 +242,25 @@ __global__ void __launch_bounds__(P2G_THREADS, 2) k_p2g(const P2GArgs a) {
 // takes the particles of the owned footprint and its one-cell ring (18 rows of
 // 32 cells, 18 contiguous runs of the cell-sorted order).  A particle's
 // contributions reach the neighbouring x-planes only, so three x-planes of
-// accumulators (7 fields: face weight and weighted velocity per axis, density,
-// over the footprint plus a two-cell margin) live in shared memory as a ring;
-// after slice x, plane x - 1 is complete: it is normalised (v / weight if the
-// weight exceeds 1e-6, else 0; WATER where a particle is; avgPNum), written
-// out and cleared for plane x + 2.  Only owned cells are written; the
+// FP32 accumulators (7 fields: face weight and weighted velocity per axis,
+// density, over the footprint plus a two-cell margin) live in shared memory as
+// a ring; after slice x, plane x - 1 is complete: it is normalised (v / weight
+// if the weight exceeds 1e-6, else 0; WATER where a particle is; avgPNum),
+// written out and cleared for plane x + 2.  Only owned cells are written; the
 // neighbouring pencil computes the others from the same ring particles (the
-// walk is 1.2x the owned cells).
+// walk is 1.2x the owned cells, against 1.58x for cubic tiles).
 //
 // Every thread takes particles of the slice and adds each particle's 56
 // contributions (8 faces on each axis, weight and weighted velocity, and 8
-// density weights; getFacesAround / getCellsAround stencils) to the ring with
-// INT32 shared-memory atomics in fixed point: weights times 2^21, weighted
-// velocities times 2^21 / 2^ceil(log2 Vmax), Vmax = the step's largest |v_a|
-// (recorded by the advection pass) + h max(1, aspect) times the largest
-// sum_b |c_ab| (recorded by G2P and uploads).  Every term is then below 2^21
-// in magnitude, is rounded to 2^-21 of the largest possible term, and integer
-// sums do not depend on the order of the atomics: P2G is reproducible bit for
-// bit.  (A plane cell gathers a few hundred terms at most -- 2^31 / 2^21 = 1024
-// would be needed to overflow.)  Lanes take particles 12 apart in the sorted
-// order, so the lanes of a warp mostly hold different cells and their atomic
-// targets rarely meet.  A particle with a non-finite position, velocity or C
-// contributes nothing; one outside its bound (which the bounds exclude) sets
-// FSIM_DERR_P2G_RANGE and contributes nothing.
+// density weights: the getFacesAround / getCellsAround stencils) with
+// shared-memory FP32 atomics.  Lanes take particles 12 apart in the sorted
+// order, so the lanes of a warp mostly hold different cells and their targets
+// rarely meet.  (A fixed-point variant with INT32 atomics, order-independent
+// and about as fast, rounded the weight sums of faces at the fluid front --
+// sums of 1e-5 -- to a few percent; FP32 keeps their relative precision.)
 //
-// Work items come from a counter (d_misc[0]); the last CTA to finish resets it,
-// the exit counter (d_misc[1]) and the velocity bound (d_misc[2]).
+// Work items come from a counter (d_misc[0]); the last CTA to finish resets it
+// and the exit counter (d_misc[1]) for the next launch.
 constexpr int FX_SY = 16;             // owned y cells per pencil
 constexpr int FX_WZ = 32;             // walk cells per row
 constexpr int FX_SZ = FX_WZ - 2;      // owned z cells per pencil
@@ -288,35 +281,19 @@ struct P2GFxArgs {
     float* u[3];
     uint8_t* flags;
     float* avg;
-    int* misc;          // [0] next item, [1] CTAs done, [2] |v| bound, [3] C bound (FP32 bits)
-    unsigned* err;
+    int* misc;          // [0] next item, [1] CTAs done
     int nsx, npy, npz;  // segments in x, pencils in y and z
     int nitems;
 };
 
-// round(x) for |x| < 2^22: adding 1.5 * 2^23 leaves the integer in the low mantissa bits
-__device__ __forceinline__ int fx_round(float x) { return __float_as_int(x + 12582912.0f) - 0x4B400000; }
-
 template <bool APIC>
 __global__ void __launch_bounds__(FX_THREADS, 2) k_p2g_fx(const P2GFxArgs a) {
-    extern __shared__ int ring[];  // [3 slots][7 fields][FX_PLANE]
+    extern __shared__ float ring[];  // [3 slots][7 fields][FX_PLANE]
     __shared__ int s_item;
     __shared__ int s_pre[FX_WY + 1], s_beg[FX_WY];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const GridGeom& g = a.g;
     const float h = g.h, zr = g.two_d ? (float)(g.hzd * g.hinvd) : 1.f;
-    // the fixed-point scales, the same for every CTA of the launch
-    const float WS = 2097152.f;  // 2^21
-    float vmax = __uint_as_float((unsigned)a.misc[2]);
-    if (APIC) vmax += h * fmaxf(1.f, zr) * __uint_as_float((unsigned)a.misc[3]);
-    vmax *= 1.001f;  // FP32 rounding of the terms
-    float VS = 1.f;
-    if (vmax > 0.f) {
-        int e;
-        frexpf(vmax, &e);  // vmax = m 2^e, 0.5 <= m < 1
-        VS = ldexpf(1.f, 21 - e);
-    }
-    const float vsw = VS / WS;
 
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(&a.misc[0], 1);
@@ -328,7 +305,7 @@ __global__ void __launch_bounds__(FX_THREADS, 2) k_p2g_fx(const P2GFxArgs a) {
         const int y0 = pyi * FX_SY, z0 = pzi * FX_SZ;
         const int ny_left = min(FX_SY, g.ny - y0), nz_left = min(FX_SZ, g.nz - z0);
         const int zlo = max(z0 - 1, 0), zhi = min(z0 - 1 + FX_WZ, g.nz);
-        for (int k = threadIdx.x; k < 3 * 7 * FX_PLANE; k += FX_THREADS) ring[k] = 0;
+        for (int k = threadIdx.x; k < 3 * 7 * FX_PLANE; k += FX_THREADS) ring[k] = 0.f;
         for (int x = xa - 1; x <= xe; x++) {
             if (x >= 0 && x < g.nx) {
                 // the slice's 18 walk rows as one list of sorted particles
@@ -376,21 +353,6 @@ __global__ void __launch_bounds__(FX_THREADS, 2) k_p2g_fx(const P2GFxArgs a) {
 #pragma unroll
                         for (int k = 0; k < 9; k++) cm[k] = a.p.c[k][i];
                     }
-                    // this particle's bound (and finiteness)
-                    float pm = 0.f;
-                    bool ok = isfinite(px) && isfinite(py) && isfinite(pz);
-#pragma unroll
-                    for (int d = 0; d < 3; d++) {
-                        float m = fabsf(v[d]);
-                        if (APIC) m += h * (fabsf(cm[3 * d]) + fabsf(cm[3 * d + 1]) + fabsf(cm[3 * d + 2]) * zr);
-                        pm = fmaxf(pm, m);
-                    }
-                    ok &= isfinite(pm);
-                    if (!ok) continue;
-                    if (pm * VS >= WS) {
-                        atomicOr(a.err, FSIM_DERR_P2G_RANGE);
-                        continue;
-                    }
                     const int cy = y0 - 1 + r;
                     const int cz = min(max((int)(pz * g.hzinv), 0), g.nz - 1);  // the sort key's z
                     const float f[3] = {px * g.hinv - (float)x, py * g.hinv - (float)cy, pz * g.hzinv - (float)cz};
@@ -404,17 +366,17 @@ __global__ void __launch_bounds__(FX_THREADS, 2) k_p2g_fx(const P2GFxArgs a) {
                         lo3[d] = low ? 0.5f - f[d] : 1.5f - f[d];
                         hi3[d] = low ? 0.5f + f[d] : f[d] - 0.5f;
                     }
-                    // ring index of cell offset (dx, dy, dz) without the field: slot + row + column
+                    // ring offset of the particle's cell within a plane
                     const int cell0 = (cy - y0 + 2) * FX_PZ + (cz - z0 + 2);
                     // density (getCellsAround + trilinear, simulator.cpp:354-368)
 #pragma unroll
                     for (int ox = 0; ox < 2; ox++)
 #pragma unroll
                         for (int oy = 0; oy < 2; oy++) {
-                            const float wxy = (ox ? hi3[0] : lo3[0]) * (oy ? hi3[1] : lo3[1]) * WS;
+                            const float wxy = (ox ? hi3[0] : lo3[0]) * (oy ? hi3[1] : lo3[1]);
                             const int e0 = slot_base[o0[0] + ox + 1] + 6 * FX_PLANE + cell0 + (o0[1] + oy) * FX_PZ + o0[2];
 #pragma unroll
-                            for (int oz = 0; oz < 2; oz++) atomicAdd(&ring[e0 + oz], fx_round(wxy * (oz ? hi3[2] : lo3[2])));
+                            for (int oz = 0; oz < 2; oz++) atomicAdd(&ring[e0 + oz], wxy * (oz ? hi3[2] : lo3[2]));
                         }
                     // faces of the three axes (getFacesAround + p2gTransfer, simulator.cpp:314-352)
 #pragma unroll
@@ -433,25 +395,24 @@ __global__ void __launch_bounds__(FX_THREADS, 2) k_p2g_fx(const P2GFxArgs a) {
                         }
                         const int strideb = b == 0 ? 0 : (b == 1 ? FX_PZ : 1);
                         const int stridec = c == 1 ? FX_PZ : 1;
-                        // offsets of the stencil's base corner: normal -1, transverse o0
+                        // the stencil's base corner: normal offset -1, transverse o0
                         const int ob_x = ax == 0 ? -1 : o0[0];
                         const int e0 = cell0 + (ax == 1 ? -1 : o0[1]) * FX_PZ + (ax == 2 ? -1 : o0[2]);
 #pragma unroll
                         for (int ii = 0; ii < 2; ii++) {
-                            const float wn = (ii ? f[ax] : 1.f - f[ax]) * WS;
+                            const float wn = ii ? f[ax] : 1.f - f[ax];
 #pragma unroll
                             for (int jb = 0; jb < 2; jb++) {
                                 const float wnb = wn * (jb ? hi3[b] : lo3[b]);
 #pragma unroll
                                 for (int jc = 0; jc < 2; jc++) {
-                                    const float w = wnb * (jc ? hi3[c] : lo3[c]);  // weight x 2^21
+                                    const float w = wnb * (jc ? hi3[c] : lo3[c]);
                                     const float val = K + ka * (float)ii + kb * (float)jb + kc * (float)jc;
-                                    // slot (x offset) and in-plane offset of this corner
                                     const int dxo = ob_x + (ax == 0 ? ii : (b == 0 ? jb : 0));
                                     const int e = slot_base[dxo + 1] + e0 + (ax == 0 ? 0 : ii * (ax == 1 ? FX_PZ : 1)) +
                                                   jb * strideb + jc * stridec;
-                                    atomicAdd(&ring[e + ax * FX_PLANE], fx_round(w * (val * vsw)));
-                                    atomicAdd(&ring[e + (3 + ax) * FX_PLANE], fx_round(w));
+                                    atomicAdd(&ring[e + ax * FX_PLANE], w * val);
+                                    atomicAdd(&ring[e + (3 + ax) * FX_PLANE], w);
                                 }
                             }
                         }
@@ -461,9 +422,8 @@ __global__ void __launch_bounds__(FX_THREADS, 2) k_p2g_fx(const P2GFxArgs a) {
             }
             // plane x - 1 is complete: write its owned cells out and clear its slot for plane x + 2
             const int xf = x - 1;
-            int* pl = ring + ((xf + 3) % 3) * 7 * FX_PLANE;
+            float* pl = ring + ((xf + 3) % 3) * 7 * FX_PLANE;
             if (xf >= xa && xf < xe) {
-                const float inv_w = 1.f / WS, inv_v = 1.f / VS;
                 for (int k = threadIdx.x; k < FX_SY * FX_SZ; k += FX_THREADS) {
                     const int ty = k / FX_SZ, tz = k - ty * FX_SZ;
                     if (ty >= ny_left || tz >= nz_left) continue;
@@ -471,25 +431,24 @@ __global__ void __launch_bounds__(FX_THREADS, 2) k_p2g_fx(const P2GFxArgs a) {
                     const long long cell = gidx(g, xf, y0 + ty, z0 + tz);
 #pragma unroll
                     for (int ax = 0; ax < 3; ax++) {
-                        const float w = (float)pl[(3 + ax) * FX_PLANE + pc] * inv_w;
-                        a.u[ax][cell] = (w > 1e-6f) ? (float)pl[ax * FX_PLANE + pc] * inv_v / w : 0.f;
+                        const float w = pl[(3 + ax) * FX_PLANE + pc];
+                        a.u[ax][cell] = (w > 1e-6f) ? pl[ax * FX_PLANE + pc] / w : 0.f;
                     }
                     a.flags[cell] = (a.cstart[cell + 1] > a.cstart[cell]) ? C_WATER : C_AIR;
-                    a.avg[cell] = (float)pl[6 * FX_PLANE + pc] * inv_w;
+                    a.avg[cell] = pl[6 * FX_PLANE + pc];
                 }
                 __syncthreads();
             }
-            for (int k = threadIdx.x; k < 7 * FX_PLANE; k += FX_THREADS) pl[k] = 0;
+            for (int k = threadIdx.x; k < 7 * FX_PLANE; k += FX_THREADS) pl[k] = 0.f;
             __syncthreads();
         }
     }
-    // the last CTA out resets the counters and the velocity bound for the next launch
+    // the last CTA out resets the counters for the next launch
     if (threadIdx.x == 0) {
         __threadfence();
         if (atomicAdd(&a.misc[1], 1) == (int)gridDim.x - 1) {
             a.misc[0] = 0;
             a.misc[1] = 0;
-            a.misc[2] = 0;
             __threadfence();
         }
     }
@@ -536,7 +495,6 @@ struct G2PArgs {
     int ids;
     int move_c;        // PIC/FLIP: carry C along the permutation
     unsigned* err;
-    unsigned* cmax;    // APIC: largest sum_b |c_ab| of the new C (FP32 bits, atomicMax; cleared before)
 };
 
 // MODE: 0 PIC, 1 FLIP, 2 APIC
@@ -640,7 +598,6 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
         }
     }
     const float hinv = a.g.hinv, hzinv = a.g.hzinv;
-    float cm_thread = 0.f;  // APIC: this thread's largest sum_b |c_ab|
     for (int j = threadIdx.x; j < total; j += blockDim.x) {
         const int k = kn;
         const uint32_t i = in;
@@ -742,20 +699,11 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
         if (MODE == 2) {
 #pragma unroll
             for (int q = 0; q < 9; q++) a.dst.c[q][k] = cnew[q];
-#pragma unroll
-            for (int r = 0; r < 3; r++) {
-                const float m = fabsf(cnew[3 * r]) + fabsf(cnew[3 * r + 1]) + fabsf(cnew[3 * r + 2]);
-                if (isfinite(m)) cm_thread = fmaxf(cm_thread, m);
-            }
         } else if (a.move_c) {
 #pragma unroll
             for (int q = 0; q < 9; q++) a.dst.c[q][k] = a.src.c[q][i];
         }
         if (a.ids) a.dst.id[k] = a.src.id[i];
-    }
-    if (MODE == 2) {
-        const unsigned mb = __reduce_max_sync(0xffffffffu, __float_as_uint(cm_thread));
-        if ((threadIdx.x & 31) == 0 && mb) atomicMax(a.cmax, mb);
     }
 }
 
@@ -772,7 +720,6 @@ void launch_p2g(fsim_ctx* ctx) {
     a.flags = ctx->flags;
     a.avg = ctx->avg;
     a.misc = ctx->d_misc;
-    a.err = ctx->d_err;
     a.nsx = ceil_div(g.nx, FX_LX);
     a.npy = ceil_div(g.ny, FX_SY);
     a.npz = ceil_div(g.nz, FX_SZ);
@@ -859,8 +806,6 @@ int launch_g2p(fsim_ctx* ctx) {
     a.ids = ctx->prm.track_ids ? 1 : 0;
     a.move_c = 1;
     a.err = ctx->d_err;
-    a.cmax = reinterpret_cast<unsigned*>(ctx->d_misc + MISC_CMAX);
-    if (ctx->prm.transfer == FSIM_APIC) cudaMemsetAsync(a.cmax, 0, sizeof(unsigned), ctx->stream);
     const int nb = a.ntx * a.nty * a.ntz;
     const int mode = ctx->prm.transfer;
     ctx->launches += 1;
