@@ -234,226 +234,6 @@ __global__ void __launch_bounds__(P2G_THREADS, 2) k_p2g(const P2GArgs a) {
     }
 }
 
-// ---- P2G: x sweep over pencils, particle-parallel shared-memory accumulation ----
-//
-// The context path's P2G.  A work item is a pencil segment: FX_SY x FX_SZ
-// owned cells in (y, z) over FX_LX owned x-slices.  The CTA sweeps the
-// segment's slices in x (plus one halo slice at each end); in each slice it
-// takes the particles of the owned footprint and its one-cell ring (18 rows of
-// 32 cells, 18 contiguous runs of the cell-sorted order).  A particle's
-// contributions reach the neighbouring x-planes only, so three x-planes of
-// FP32 accumulators (7 fields: face weight and weighted velocity per axis,
-// density, over the footprint plus a two-cell margin) live in shared memory as
-// a ring; after slice x, plane x - 1 is complete: it is normalised (v / weight
-// if the weight exceeds 1e-6, else 0; WATER where a particle is; avgPNum),
-// written out and cleared for plane x + 2.  Only owned cells are written; the
-// neighbouring pencil computes the others from the same ring particles (the
-// walk is 1.2x the owned cells, against 1.58x for cubic tiles).
-//
-// Every thread takes particles of the slice and adds each particle's 56
-// contributions (8 faces on each axis, weight and weighted velocity, and 8
-// density weights: the getFacesAround / getCellsAround stencils) with
-// shared-memory FP32 atomics.  Lanes take particles 12 apart in the sorted
-// order, so the lanes of a warp mostly hold different cells and their targets
-// rarely meet.  (A fixed-point variant with INT32 atomics, order-independent
-// and about as fast, rounded the weight sums of faces at the fluid front --
-// sums of 1e-5 -- to a few percent; FP32 keeps their relative precision.)
-//
-// Work items come from a counter (d_misc[0]); the last CTA to finish resets it
-// and the exit counter (d_misc[1]) for the next launch.
-constexpr int FX_SY = 16;             // owned y cells per pencil
-constexpr int FX_WZ = 32;             // walk cells per row
-constexpr int FX_SZ = FX_WZ - 2;      // owned z cells per pencil
-constexpr int FX_WY = FX_SY + 2;      // walk rows per slice
-constexpr int FX_LX = 32;             // owned x slices per work item
-constexpr int FX_THREADS = 384;
-constexpr int FX_WARPS = FX_THREADS / 32;
-constexpr int FX_PY = FX_SY + 4;      // plane rows: y0 - 2 .. y0 + SY + 1
-constexpr int FX_PZ = FX_SZ + 4;      // plane columns: z0 - 2 .. z0 + SZ + 1
-constexpr int FX_PLANE = FX_PY * FX_PZ;
-constexpr int FX_SMEM = 3 * 7 * FX_PLANE * 4;
-
-struct P2GFxArgs {
-    ParticleBuf p;
-    const uint32_t* perm;
-    const int* cstart;
-    GridGeom g;
-    float* u[3];
-    uint8_t* flags;
-    float* avg;
-    int* misc;          // [0] next item, [1] CTAs done
-    int nsx, npy, npz;  // segments in x, pencils in y and z
-    int nitems;
-};
-
-template <bool APIC>
-__global__ void __launch_bounds__(FX_THREADS, 2) k_p2g_fx(const P2GFxArgs a) {
-    extern __shared__ float ring[];  // [3 slots][7 fields][FX_PLANE]
-    __shared__ int s_item;
-    __shared__ int s_pre[FX_WY + 1], s_beg[FX_WY];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const GridGeom& g = a.g;
-    const float h = g.h, zr = g.two_d ? (float)(g.hzd * g.hinvd) : 1.f;
-
-    for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(&a.misc[0], 1);
-        __syncthreads();
-        const int item = s_item;
-        if (item >= a.nitems) break;
-        const int pzi = item % a.npz, pyi = (item / a.npz) % a.npy, sxi = item / (a.npz * a.npy);
-        const int xa = sxi * FX_LX, xe = min(xa + FX_LX, g.nx);
-        const int y0 = pyi * FX_SY, z0 = pzi * FX_SZ;
-        const int ny_left = min(FX_SY, g.ny - y0), nz_left = min(FX_SZ, g.nz - z0);
-        const int zlo = max(z0 - 1, 0), zhi = min(z0 - 1 + FX_WZ, g.nz);
-        for (int k = threadIdx.x; k < 3 * 7 * FX_PLANE; k += FX_THREADS) ring[k] = 0.f;
-        for (int x = xa - 1; x <= xe; x++) {
-            if (x >= 0 && x < g.nx) {
-                // the slice's 18 walk rows as one list of sorted particles
-                if (warp == 0) {
-                    const int y = y0 - 1 + lane;
-                    int beg = 0, len = 0;
-                    if (lane < FX_WY && y >= 0 && y < g.ny) {
-                        const long long rowc = gidx(g, x, y, 0);
-                        beg = a.cstart[rowc + zlo];
-                        len = a.cstart[rowc + zhi] - beg;
-                    }
-                    int incl = len;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int t = __shfl_up_sync(0xffffffffu, incl, o);
-                        if (lane >= o) incl += t;
-                    }
-                    if (lane < FX_WY) {
-                        s_beg[lane] = beg;
-                        s_pre[lane + 1] = incl;
-                    }
-                    if (lane == 0) s_pre[0] = 0;
-                }
-                __syncthreads();
-                const int total = s_pre[FX_WY];
-                const int slot_base[3] = {((x + 2) % 3) * 7 * FX_PLANE, ((x + 3) % 3) * 7 * FX_PLANE,
-                                          ((x + 4) % 3) * 7 * FX_PLANE};  // planes x - 1, x, x + 1
-                for (int base = 0; base < total; base += FX_THREADS) {
-                    const int j = base + lane * FX_WARPS + warp;  // lanes 12 particles apart
-                    if (j >= total) continue;
-                    int lo = 0, hi = FX_WY;  // the row r with s_pre[r] <= j < s_pre[r + 1]
-#pragma unroll
-                    for (int step = 0; step < 5; step++) {
-                        const int mid = (lo + hi) >> 1;
-                        if (mid < FX_WY && s_pre[mid] <= j) lo = mid;
-                        else hi = mid;
-                    }
-                    const int r = lo;
-                    const uint32_t i = a.perm[s_beg[r] + (j - s_pre[r])];
-                    const float px = a.p.p[0][i], py = a.p.p[1][i], pz = a.p.p[2][i];
-                    float v[3], cm[9];
-#pragma unroll
-                    for (int d = 0; d < 3; d++) v[d] = a.p.v[d][i];
-                    if (APIC) {
-#pragma unroll
-                        for (int k = 0; k < 9; k++) cm[k] = a.p.c[k][i];
-                    }
-                    const int cy = y0 - 1 + r;
-                    const int cz = min(max((int)(pz * g.hzinv), 0), g.nz - 1);  // the sort key's z
-                    const float f[3] = {px * g.hinv - (float)x, py * g.hinv - (float)cy, pz * g.hzinv - (float)cz};
-                    float lo3[3], hi3[3];
-                    int o0[3];
-#pragma unroll
-                    for (int d = 0; d < 3; d++) {
-                        // the two non-zero tent weights of the cell-centred nodes at o0, o0 + 1
-                        const bool low = f[d] < 0.5f;
-                        o0[d] = low ? -1 : 0;
-                        lo3[d] = low ? 0.5f - f[d] : 1.5f - f[d];
-                        hi3[d] = low ? 0.5f + f[d] : f[d] - 0.5f;
-                    }
-                    // ring offset of the particle's cell within a plane
-                    const int cell0 = (cy - y0 + 2) * FX_PZ + (cz - z0 + 2);
-                    // density (getCellsAround + trilinear, simulator.cpp:354-368)
-#pragma unroll
-                    for (int ox = 0; ox < 2; ox++)
-#pragma unroll
-                        for (int oy = 0; oy < 2; oy++) {
-                            const float wxy = (ox ? hi3[0] : lo3[0]) * (oy ? hi3[1] : lo3[1]);
-                            const int e0 = slot_base[o0[0] + ox + 1] + 6 * FX_PLANE + cell0 + (o0[1] + oy) * FX_PZ + o0[2];
-#pragma unroll
-                            for (int oz = 0; oz < 2; oz++) atomicAdd(&ring[e0 + oz], wxy * (oz ? hi3[2] : lo3[2]));
-                        }
-                    // faces of the three axes (getFacesAround + p2gTransfer, simulator.cpp:314-352)
-#pragma unroll
-                    for (int ax = 0; ax < 3; ax++) {
-                        const int b = ax == 0 ? 1 : 0, c = ax == 2 ? 1 : 2;
-                        // v_a + c_a . (face - pos): face - pos = h (ii - f_a) along a and
-                        // h (o + 0.5 - f) across (z terms scaled by zr in 2D mode)
-                        float K = v[ax], ka = 0.f, kb = 0.f, kc = 0.f;
-                        if (APIC) {
-                            const float* ca = cm + 3 * ax;
-                            K -= h * (ca[0] * f[0] + ca[1] * f[1] + ca[2] * f[2] * zr);
-                            ka = h * ca[ax] * (ax == 2 ? zr : 1.f);
-                            kb = h * ca[b];
-                            kc = h * ca[c] * (c == 2 ? zr : 1.f);
-                            K += kb * ((float)o0[b] + 0.5f) + kc * ((float)o0[c] + 0.5f);
-                        }
-                        const int strideb = b == 0 ? 0 : (b == 1 ? FX_PZ : 1);
-                        const int stridec = c == 1 ? FX_PZ : 1;
-                        // the stencil's base corner: normal offset -1, transverse o0
-                        const int ob_x = ax == 0 ? -1 : o0[0];
-                        const int e0 = cell0 + (ax == 1 ? -1 : o0[1]) * FX_PZ + (ax == 2 ? -1 : o0[2]);
-#pragma unroll
-                        for (int ii = 0; ii < 2; ii++) {
-                            const float wn = ii ? f[ax] : 1.f - f[ax];
-#pragma unroll
-                            for (int jb = 0; jb < 2; jb++) {
-                                const float wnb = wn * (jb ? hi3[b] : lo3[b]);
-#pragma unroll
-                                for (int jc = 0; jc < 2; jc++) {
-                                    const float w = wnb * (jc ? hi3[c] : lo3[c]);
-                                    const float val = K + ka * (float)ii + kb * (float)jb + kc * (float)jc;
-                                    const int dxo = ob_x + (ax == 0 ? ii : (b == 0 ? jb : 0));
-                                    const int e = slot_base[dxo + 1] + e0 + (ax == 0 ? 0 : ii * (ax == 1 ? FX_PZ : 1)) +
-                                                  jb * strideb + jc * stridec;
-                                    atomicAdd(&ring[e + ax * FX_PLANE], w * val);
-                                    atomicAdd(&ring[e + (3 + ax) * FX_PLANE], w);
-                                }
-                            }
-                        }
-                    }
-                }
-                __syncthreads();
-            }
-            // plane x - 1 is complete: write its owned cells out and clear its slot for plane x + 2
-            const int xf = x - 1;
-            float* pl = ring + ((xf + 3) % 3) * 7 * FX_PLANE;
-            if (xf >= xa && xf < xe) {
-                for (int k = threadIdx.x; k < FX_SY * FX_SZ; k += FX_THREADS) {
-                    const int ty = k / FX_SZ, tz = k - ty * FX_SZ;
-                    if (ty >= ny_left || tz >= nz_left) continue;
-                    const int pc = (ty + 2) * FX_PZ + tz + 2;
-                    const long long cell = gidx(g, xf, y0 + ty, z0 + tz);
-#pragma unroll
-                    for (int ax = 0; ax < 3; ax++) {
-                        const float w = pl[(3 + ax) * FX_PLANE + pc];
-                        a.u[ax][cell] = (w > 1e-6f) ? pl[ax * FX_PLANE + pc] / w : 0.f;
-                    }
-                    a.flags[cell] = (a.cstart[cell + 1] > a.cstart[cell]) ? C_WATER : C_AIR;
-                    a.avg[cell] = pl[6 * FX_PLANE + pc];
-                }
-                __syncthreads();
-            }
-            for (int k = threadIdx.x; k < 7 * FX_PLANE; k += FX_THREADS) pl[k] = 0.f;
-            __syncthreads();
-        }
-    }
-    // the last CTA out resets the counters for the next launch
-    if (threadIdx.x == 0) {
-        __threadfence();
-        if (atomicAdd(&a.misc[1], 1) == (int)gridDim.x - 1) {
-            a.misc[0] = 0;
-            a.misc[1] = 0;
-            __threadfence();
-        }
-    }
-}
-
 // ---- TMA / mbarrier helpers (inline PTX) ------------------------------------
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return (unsigned)__cvta_generic_to_shared(p);
@@ -711,7 +491,7 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
 
 void launch_p2g(fsim_ctx* ctx) {
     const GridGeom& g = ctx->g;
-    P2GFxArgs a;
+    P2GArgs a;
     a.p = ctx->buf[ctx->cur];
     a.perm = ctx->perm;
     a.cstart = ctx->cstart;
@@ -719,20 +499,17 @@ void launch_p2g(fsim_ctx* ctx) {
     for (int k = 0; k < 3; k++) a.u[k] = ctx->u[k];
     a.flags = ctx->flags;
     a.avg = ctx->avg;
-    a.misc = ctx->d_misc;
-    a.nsx = ceil_div(g.nx, FX_LX);
-    a.npy = ceil_div(g.ny, FX_SY);
-    a.npz = ceil_div(g.nz, FX_SZ);
-    a.nitems = a.nsx * a.npy * a.npz;
-    const int grid = std::min(a.nitems, 2 * ctx->num_sms);
+    a.ntx = ceil_div(g.nx, PX);
+    a.nty = ceil_div(g.ny, PY);
+    a.ntz = ceil_div(g.nz, PZ);
+    const int nb = a.ntx * a.nty * a.ntz;
     ctx->launches += 1;
-    if (ctx->prm.transfer == FSIM_APIC) {
-        set_smem_limit((const void*)k_p2g_fx<true>, FX_SMEM);
-        k_p2g_fx<true><<<grid, FX_THREADS, FX_SMEM, ctx->stream>>>(a);
-    } else {
-        set_smem_limit((const void*)k_p2g_fx<false>, FX_SMEM);
-        k_p2g_fx<false><<<grid, FX_THREADS, FX_SMEM, ctx->stream>>>(a);
-    }
+    set_smem_limit((const void*)k_p2g<false>, P2G_SMEM);
+    set_smem_limit((const void*)k_p2g<true>, P2G_SMEM);
+    if (ctx->prm.transfer == FSIM_APIC)
+        k_p2g<true><<<nb, P2G_THREADS, P2G_SMEM, ctx->stream>>>(a);
+    else
+        k_p2g<false><<<nb, P2G_THREADS, P2G_SMEM, ctx->stream>>>(a);
 }
 
 // P2G on caller-provided buffers (used by the allocation-free entry point in
