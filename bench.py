@@ -594,7 +594,8 @@ def precision_study(sim, N, seed: int = 11):
 
 # ---------------------------------------------------------------- learned warm start
 WARMSTART_WEIGHTS = os.path.join(ROOT, "fluid_simulator_gb300", "weights", "warmstart_c5.npz")
-STARTS = (("zero", 0), ("previous", 1), ("learned", 3))   # FSIM_WARM_ZERO / _PREVIOUS / _LEARNED
+# FSIM_WARM_ZERO / _PREVIOUS / _LEARNED / _LEARNED_RESIDUAL
+STARTS = (("zero", 0), ("previous", 1), ("learned", 3), ("learned_residual", 4))
 PRECONDS = (("rbic", 0), ("mg", 1))                      # FSIM_PRECOND_RBIC (the plain solver) / _MG
 
 
@@ -635,12 +636,13 @@ def compare_starts(sim, dt, N, stages_fn, problems: int, max_iters: int = 20000)
                        "iterations": round(statistics.mean(x[1] for x in r), 2),
                        "residual_rel_max": float(f"{max(x[4] for x in r):.3g}"),
                        "converged": all(x[5] == 1 for x in r)}
-        lr = rec[(pn, "learned")]
-        row["learned"]["guess_used_frac"] = round(sum(1 for x in lr if x[2] == 3) / len(lr), 3)
-        row["learned"]["fallback_rate"] = round(1.0 - row["learned"]["guess_used_frac"], 3)
-        row["learned"]["ms_inference"] = round(statistics.mean(x[3] for x in lr), 3)
-        row["speedup_learned_vs_zero"] = round(row["zero"]["ms"] / row["learned"]["ms"], 3)
-        row["speedup_learned_vs_previous"] = round(row["previous"]["ms"] / row["learned"]["ms"], 3)
+        for sn, mode in (("learned", 3), ("learned_residual", 4)):
+            lr = rec[(pn, sn)]
+            row[sn]["guess_used_frac"] = round(sum(1 for x in lr if x[2] == mode) / len(lr), 3)
+            row[sn]["fallback_rate"] = round(1.0 - row[sn]["guess_used_frac"], 3)
+            row[sn]["ms_inference"] = round(statistics.mean(x[3] for x in lr), 3)
+            row[f"speedup_{sn}_vs_zero"] = round(row["zero"]["ms"] / row[sn]["ms"], 3)
+            row[f"speedup_{sn}_vs_previous"] = round(row["previous"]["ms"] / row[sn]["ms"], 3)
         row["speedup_previous_vs_zero"] = round(row["zero"]["ms"] / row["previous"]["ms"], 3)
         out[pn] = row
     return out

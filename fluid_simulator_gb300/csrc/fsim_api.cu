@@ -383,6 +383,10 @@ int validate_params(const fsim_params* p, std::string& why) {
     if (!(p->fluid_density > 0)) { why = "fluid_density"; return FSIM_E_INVALID; }
     if (p->precision < FSIM_PREC_MIXED || p->precision > FSIM_PREC_FP64) { why = "precision"; return FSIM_E_INVALID; }
     if (p->tol_mode != FSIM_TOL_ABS_MAX && p->tol_mode != FSIM_TOL_REL_L2) { why = "tol_mode"; return FSIM_E_INVALID; }
+    if (p->warm_start < FSIM_WARM_ZERO || p->warm_start > FSIM_WARM_LEARNED_RESIDUAL) {
+        why = "warm_start";
+        return FSIM_E_INVALID;
+    }
     return FSIM_OK;
 }
 
@@ -1023,7 +1027,8 @@ int fsim_set_pressure_guess(fsim_ctx* ctx, const float* p, int where) {
 }
 
 int fsim_solve_current(fsim_ctx* ctx, double dt, int warm_start, int apply, fsim_step_stats* stats) {
-    if (!ctx || !(dt > 0) || warm_start < FSIM_WARM_ZERO || warm_start > FSIM_WARM_LEARNED) return FSIM_E_INVALID;
+    if (!ctx || !(dt > 0) || warm_start < FSIM_WARM_ZERO || warm_start > FSIM_WARM_LEARNED_RESIDUAL)
+        return FSIM_E_INVALID;
     const fsim_params& P = ctx->prm;
     cudaStream_t s = ctx->stream;
     fsim_step_stats tmp{};

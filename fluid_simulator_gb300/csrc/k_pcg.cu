@@ -1957,6 +1957,35 @@ __global__ void __launch_bounds__(PCG_THREADS) k_guess_judge(const PcgArgs a, co
     }
 }
 
+// r = b - A phi in FP64 on the fluid cells of the active bricks (0 elsewhere):
+// the rhs of the correction the previous pressure still needs
+__global__ void __launch_bounds__(PCG_THREADS) k_prev_residual(const PcgArgs a, double* r) {
+    const int nact = *a.nactive;
+    for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
+        int x, y, z;
+        long long c;
+        if (!brick_cell(a.B, a.bxyz[bk], threadIdx.x, x, y, z, c)) continue;
+        const uint16_t cc = a.code[c];
+        if (!(cc & CODE_FLUID)) continue;
+        double ap = (double)code_ns(cc) * a.phi[c];
+#pragma unroll
+        for (int k = 0; k < 6; k++)
+            if ((cc >> k) & 1) ap -= a.phi[c + nb_off(a.B, k)];
+        r[c] = a.b[c] - ap;
+    }
+}
+
+// guess = phi + correction on the fluid cells of the active bricks
+__global__ void __launch_bounds__(PCG_THREADS) k_guess_add_prev(const PcgArgs a, float* guess) {
+    const int nact = *a.nactive;
+    for (int bk = blockIdx.x; bk < nact; bk += gridDim.x) {
+        int x, y, z;
+        long long c;
+        if (!brick_cell(a.B, a.bxyz[bk], threadIdx.x, x, y, z, c)) continue;
+        if (a.code[c] & CODE_FLUID) guess[c] = (float)(a.phi[c] + (double)guess[c]);
+    }
+}
+
 __global__ void __launch_bounds__(PCG_THREADS) k_guess_apply(const PcgArgs a, const float* guess) {
     if (!a.st->guess_used) return;
     const int nact = *a.nactive;
@@ -2153,18 +2182,20 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     sa.flags = ctx->flags;
     for (int a = 0; a < 3; a++) sa.v2[a] = ctx->v2[a];
     sa.avg = ctx->avg;
-    if (warm == FSIM_WARM_LEARNED && !ctx->net) {
-        ctx->err = "FSIM_WARM_LEARNED needs a network (fsim_set_net)";
+    const bool learned = warm == FSIM_WARM_LEARNED || warm == FSIM_WARM_LEARNED_RESIDUAL;
+    if (learned && !ctx->net) {
+        ctx->err = "FSIM_WARM_LEARNED / _LEARNED_RESIDUAL need a network (fsim_set_net)";
         return FSIM_E_STATE;
     }
     // back-off: a network whose guesses keep losing to the previous pressure is
     // skipped (not run) for a growing number of solves
-    if (warm == FSIM_WARM_LEARNED && ctx->prm.learned_backoff && ctx->learned_skip > 0) {
+    if (learned && ctx->prm.learned_backoff && ctx->learned_skip > 0) {
         ctx->learned_skip--;
         warm = FSIM_WARM_PREVIOUS;
     }
     // a user or learned guess is judged against the previous pressure after setup
-    const bool judged = warm == FSIM_WARM_LEARNED || (warm == FSIM_WARM_GUESS && S.have_guess);
+    const bool judged = warm == FSIM_WARM_LEARNED || warm == FSIM_WARM_LEARNED_RESIDUAL ||
+                        (warm == FSIM_WARM_GUESS && S.have_guess);
     sa.guess = nullptr;
     sa.rhs_override = rhs_override;
     sa.warm = (warm == FSIM_WARM_ZERO) ? FSIM_WARM_ZERO : FSIM_WARM_PREVIOUS;
@@ -2220,6 +2251,20 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
                 ctx->err = std::string("warm-start network: ") + fsim_net_last_error(ctx->net);
                 return rc;
             }
+        } else if (warm == FSIM_WARM_LEARNED_RESIDUAL) {
+            // the network answers the residual of the previous pressure; its answer
+            // is added to that pressure (FP64 scratch: the FP64 solver's r buffer)
+            if ((rc = alloc_fp64(ctx))) return rc;
+            FSIM_CUDA_TRY(ctx, cudaMemsetAsync(S.r64, 0, (size_t)g.ncell * sizeof(double), st));
+            k_prev_residual<<<S.grid_blocks, PCG_THREADS, 0, st>>>(A, S.r64);
+            const long long l0 = ctx->net->launches;
+            rc = net_guess(ctx->net, g, S.code, ctx->flags, S.r64, S.guess, st);
+            ctx->launches += ctx->net->launches - l0 + 2;
+            if (rc) {
+                ctx->err = std::string("warm-start network: ") + fsim_net_last_error(ctx->net);
+                return rc;
+            }
+            k_guess_add_prev<<<S.grid_blocks, PCG_THREADS, 0, st>>>(A, S.guess);
         }
         k_guess_judge<<<S.grid_blocks, PCG_THREADS, 0, st>>>(A, S.guess);
         k_guess_apply<<<S.grid_blocks, PCG_THREADS, 0, st>>>(A, S.guess);
@@ -2246,7 +2291,7 @@ int solve_pressure(fsim_ctx* ctx, double dt, int precision, int tol_mode, double
     }
     if (rc) return rc;
     PcgState& hs = *S.st_host;
-    if (warm == FSIM_WARM_LEARNED && ctx->prm.learned_backoff) {
+    if (learned && warm != FSIM_WARM_PREVIOUS && ctx->prm.learned_backoff) {
         if (hs.guess_used) {
             ctx->learned_wait = 0;
         } else {

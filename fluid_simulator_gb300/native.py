@@ -22,7 +22,7 @@ HOST, DEVICE = 0, 1
 OBS_SPHERE, OBS_BOX, OBS_SOURCE, OBS_SINK, OBS_DISC_SOURCE, OBS_BOX_SINK = range(6)
 TOL_ABS_MAX, TOL_REL_L2 = 0, 1
 PREC_MIXED, PREC_FP32, PREC_FP64 = 0, 1, 2
-WARM_ZERO, WARM_PREVIOUS, WARM_GUESS, WARM_LEARNED = 0, 1, 2, 3
+WARM_ZERO, WARM_PREVIOUS, WARM_GUESS, WARM_LEARNED, WARM_LEARNED_RESIDUAL = 0, 1, 2, 3, 4
 PRECOND_RBIC, PRECOND_MG = 0, 1
 SOLVER_PCG, SOLVER_SOR = 0, 1
 (STAGE_SPAWN, STAGE_ADVECT, STAGE_PUSH_APART, STAGE_PUSH_OUT, STAGE_STOP, STAGE_P2G, STAGE_MARK,

@@ -93,9 +93,13 @@ enum fsim_warm_start {
     FSIM_WARM_PREVIOUS = 1, /* previous step's pressure */
     FSIM_WARM_GUESS = 2,    /* fsim_set_pressure_guess, falling back to the previous step's
                                pressure when the guess has the larger residual */
-    FSIM_WARM_LEARNED = 3   /* the attached warm-start network (fsim_set_net), falling back
+    FSIM_WARM_LEARNED = 3,  /* the attached warm-start network (fsim_set_net), falling back
                                to the previous step's pressure when its guess has the larger
                                residual */
+    FSIM_WARM_LEARNED_RESIDUAL = 4 /* the previous step's pressure plus the network's answer to
+                               the residual that pressure leaves (b - A p_prev, the same kind of
+                               Poisson problem), falling back to the previous pressure alone
+                               when the sum has the larger residual */
 };
 
 /* Step stages, in the order Simulator::simulate runs them (simulator.cpp:51-100). */
