@@ -307,6 +307,255 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv_mma(const MmaArgs a, cons
 }
 
 // ---------------------------------------------------------------------------
+// forward / input-gradient of the 3x3x3 layers: persistent, warp-specialized
+// ---------------------------------------------------------------------------
+// One CTA per SM walks the output tiles t = blockIdx.x, + gridDim.x, ...  Warp
+// 0 (one thread) streams (tile, 16-channel chunk) items into a ring of shared
+// memory stages with TMA, warp 1 (one thread) issues each item's 108 MMAs into
+// one of two TMEM accumulators, and warps 2-5 drain the other accumulator
+// (bias, ReLU or mask, BF16 stores) while the next tile accumulates, so loads,
+// MMAs and the epilogue of neighbouring tiles overlap instead of running one
+// after the other in every CTA.  When the layer has one N tile and its
+// weights fit beside two stages, all chunks' weights are loaded once and stay
+// resident; otherwise each stage carries its chunk's weights as above.
+// Every wait is bounded; a timeout (or a role that gave up) makes all roles
+// stop, the copies in flight land, the issued MMAs finish, TMEM is freed.
+constexpr int PERS_THREADS = 192;
+constexpr int PERS_MAX_STAGES = 4;
+
+struct PersArgs {
+    MmaArgs m;
+    int total_tiles;  // tiles_w * tiles_h * tiles_d * n * ntiles
+    int wres;         // weights of all chunks resident in shared memory
+    int stage_bytes;  // halo box (plus the chunk's weights when not resident)
+    int ncols;        // TMEM columns of one accumulator
+};
+
+struct TileAt {
+    int w0, h0, d0, nb, n0;
+};
+
+__device__ __forceinline__ TileAt tile_at(const MmaArgs& a, int t) {
+    TileAt c;
+    const int nti = t % a.ntiles;
+    t /= a.ntiles;
+    c.w0 = (t % a.tiles_w) * TW;
+    t /= a.tiles_w;
+    c.h0 = (t % a.tiles_h) * TH;
+    t /= a.tiles_h;
+    c.d0 = (t % a.tiles_d) * TD;
+    c.nb = t / a.tiles_d;
+    c.n0 = nti * a.nt;
+    return c;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(s32(bar)) : "memory");
+}
+// bounded wait that also gives up once another role has stopped
+__device__ __forceinline__ bool mbar_wait_ab(uint64_t* bar, unsigned phase, volatile int* stop, unsigned* err) {
+    const long long t0 = clock64();
+    while (!mbar_try(bar, phase)) {
+        if (*stop) return false;
+        if (clock64() - t0 > SPIN_LIMIT) {
+            *stop = 1;
+            atomicOr(err, 1u);
+            return false;
+        }
+    }
+    return true;
+}
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+
+__global__ void __launch_bounds__(PERS_THREADS, 1) k_conv_pers(const PersArgs p, const __grid_constant__ CUtensorMap tx,
+                                                                const __grid_constant__ CUtensorMap tw) {
+    using G = Halo<27>;
+    const MmaArgs& a = p.m;
+    extern __shared__ __align__(128) unsigned char smraw[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 127) & ~(uintptr_t)127);
+    __shared__ __align__(8) uint64_t full[PERS_MAX_STAGES], empty[PERS_MAX_STAGES], acc_full[2], acc_empty[2];
+    __shared__ __align__(8) uint64_t wfull, done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_stop, s_issued, s_consumed;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int S = a.stages;
+    const int nchunk = a.cin >> 4;
+    const int B_KC = 27 * a.nt * 16;
+    unsigned char* wbase = sm + S * p.stage_bytes;
+    const int my_tiles = (int)blockIdx.x < p.total_tiles ? (p.total_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int items = my_tiles * nchunk;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4);
+        }
+        mbar_init(&wfull, 1);
+        mbar_init(&done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_stop = 0;
+        s_issued = 0;
+        s_consumed = 0;
+    }
+    if (warp == 0) tmem_alloc(&tmem_base, 2 * p.ncols);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_base;
+    volatile int* stop = &s_stop;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            if (p.wres) {
+                mbar_expect_tx(&wfull, (unsigned)(nchunk * 2 * B_KC));
+                for (int k = 0; k < nchunk; k++)
+                    for (int kc = 0; kc < 2; kc++) tma_3d(wbase + (k * 2 + kc) * B_KC, &tw, k * 16 + kc * 8, 0, 0, &wfull);
+            }
+            int issued = 0;
+            for (int j = 0; j < items; j++) {
+                const int s = j % S;
+                if (j >= S && !mbar_wait_ab(&empty[s], (unsigned)(((j / S) - 1) & 1), stop, a.err)) break;
+                const TileAt c = tile_at(a, (int)blockIdx.x + (j / nchunk) * (int)gridDim.x);
+                const int k = j % nchunk;
+                unsigned char* st = sm + s * p.stage_bytes;
+                mbar_expect_tx(&full[s], (unsigned)p.stage_bytes);
+#pragma unroll
+                for (int kc = 0; kc < 2; kc++) {
+                    tma_5d(st + kc * G::KC, &tx, k * 16 + kc * 8, c.w0 - 1, c.h0 - 1, c.d0 - 1, c.nb, &full[s]);
+                    if (!p.wres) tma_3d(st + G::A_BYTES + kc * B_KC, &tw, k * 16 + kc * 8, c.n0, 0, &full[s]);
+                }
+                issued = j + 1;
+            }
+            s_issued = issued;
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(a.nt);
+            bool ok = !p.wres || mbar_wait_ab(&wfull, 0, stop, a.err);
+            int consumed = 0;
+            for (int j = 0; ok && j < items; j++) {
+                const int s = j % S, ti = j / nchunk, k = j % nchunk, buf = ti & 1;
+                if (!mbar_wait_ab(&full[s], (unsigned)((j / S) & 1), stop, a.err)) break;
+                consumed = j + 1;
+                if (k == 0 && ti >= 2 && !mbar_wait_ab(&acc_empty[buf], (unsigned)(((ti >> 1) - 1) & 1), stop, a.err))
+                    break;
+                fence_after();
+                const uint32_t abase = s32(sm + s * p.stage_bytes);
+                const uint32_t bbase = p.wres ? s32(wbase + k * 2 * B_KC) : abase + G::A_BYTES;
+                // The 108 MMAs are unrolled with their descriptors formed by
+                // adding to two base descriptors (the start-address field is
+                // the byte address / 16, so a shift by `row` halo rows adds
+                // `row` and the next tap's weights add nt): one thread issues
+                // every MMA of the CTA and must not spend more time per MMA
+                // than the tensor core does.
+                const uint64_t ad0 = sdesc(abase, (uint32_t)G::KC, (uint32_t)(G::AW * 16));
+                const int bstep = a.flip ? -a.nt : a.nt;
+                const uint64_t bd0 = sdesc(bbase, (uint32_t)B_KC, 128) + (uint64_t)(a.flip ? 26 * a.nt : 0);
+                const uint32_t acc0 = tmem + (uint32_t)(buf * p.ncols);
+                const uint32_t accz[TD] = {acc0, acc0 + (uint32_t)a.nt, acc0 + (uint32_t)(2 * a.nt),
+                                           acc0 + (uint32_t)(3 * a.nt)};
+#pragma unroll
+                for (int tap = 0; tap < 27; tap++) {
+                    const int kd = tap / 9, kh = (tap / 3) % 3, kw = tap % 3;
+                    const uint64_t bdesc = bd0 + (uint64_t)(long long)(tap * bstep);
+#pragma unroll
+                    for (int zp = 0; zp < TD; zp++) {
+                        const int row = ((zp + kd) * G::AH + kh) * G::AW + kw;
+                        mma_bf16(accz[zp], ad0 + (uint64_t)row, bdesc, idesc, (k > 0 || tap > 0) ? 1u : 0u);
+                    }
+                }
+                mma_commit(&empty[s]);
+                if (k == nchunk - 1) mma_commit(&acc_full[buf]);
+            }
+            s_consumed = consumed;
+            mma_commit(&done);  // arrives once every MMA issued above has completed
+        }
+    } else {
+        const int q = warp & 3;  // the TMEM lane quarter this warp may access
+        const int m = q * 32 + lane;
+        for (int ti = 0; ti < my_tiles; ti++) {
+            const int buf = ti & 1;
+            if (!mbar_wait_ab(&acc_full[buf], (unsigned)((ti >> 1) & 1), stop, a.err)) break;
+            fence_after();
+            const TileAt c = tile_at(a, (int)blockIdx.x + ti * (int)gridDim.x);
+            const int vw = c.w0 + (m & 7), vh = c.h0 + (m >> 3);
+            const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * p.ncols);
+#pragma unroll 1
+            for (int zp = 0; zp < TD; zp++) {
+                const int vd = c.d0 + zp;
+                const bool inside = vw < a.w && vh < a.h && vd < a.d;
+                const long long vox = (((long long)c.nb * a.d + vd) * a.h + vh) * a.w + vw;
+#pragma unroll 1
+                for (int c0 = 0; c0 < a.nt; c0 += 32) {
+                    // two 16-column loads in flight before one wait (nt is 16, 32 or 64)
+                    uint32_t r[2][16];
+                    const int nh = a.nt - c0 >= 32 ? 2 : 1;
+                    tmem_ld16_async(lane_addr + (uint32_t)(zp * a.nt + c0), r[0]);
+                    if (nh == 2) tmem_ld16_async(lane_addr + (uint32_t)(zp * a.nt + c0 + 16), r[1]);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    if (!inside) continue;
+#pragma unroll
+                    for (int hh = 0; hh < 2; hh++) {
+                        if (hh >= nh) break;
+                        const int ch = c.n0 + c0 + hh * 16;
+                        float v[16];
+#pragma unroll
+                        for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[hh][j]);
+                        if (a.bias) {
+#pragma unroll
+                            for (int j = 0; j < 16; j++) v[j] += a.bias[ch + j];
+                        }
+                        if (a.relu) {
+#pragma unroll
+                            for (int j = 0; j < 16; j++) v[j] = fmaxf(v[j], 0.f);
+                        }
+                        if (a.mask) {
+                            const uint4* mp = reinterpret_cast<const uint4*>(a.mask + vox * a.ms + a.mo + ch);
+                            uint4 mv[2] = {mp[0], mp[1]};
+                            const unsigned short* mb = reinterpret_cast<const unsigned short*>(mv);
+#pragma unroll
+                            for (int j = 0; j < 16; j++)
+                                if (!bf16_pos(mb[j])) v[j] = 0.f;
+                        }
+                        __align__(16) __nv_bfloat162 o[8];
+#pragma unroll
+                        for (int j = 0; j < 8; j++) o[j] = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+                        uint4* dst = reinterpret_cast<uint4*>(a.y + vox * a.ys + a.yo + ch);
+                        dst[0] = reinterpret_cast<const uint4*>(o)[0];
+                        dst[1] = reinterpret_cast<const uint4*>(o)[1];
+                    }
+                }
+            }
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[buf]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 32 && !mbar_wait(&done, 0)) atomicOr(a.err, 2u);
+    if (threadIdx.x == 0 && s_stop) {
+        // let the copies still in flight land before the CTA's shared memory goes away
+        for (int j = s_consumed; j < s_issued; j++) mbar_wait(&full[j % S], (unsigned)((j / S) & 1));
+        if (p.wres) mbar_wait(&wfull, 0);
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_free(tmem, 2 * p.ncols);
+}
+
+// ---------------------------------------------------------------------------
 // weight gradient
 // ---------------------------------------------------------------------------
 constexpr int WG_MAX_MT = 8;
@@ -513,27 +762,54 @@ int launch_conv_mma(const ConvLaunch& L, cudaStream_t s) {
     a.mask = L.mask; a.ms = L.ms; a.mo = L.mo;
     a.y = L.y; a.ys = L.ys; a.yo = L.yo;
     a.err = L.err;
-    const int a_bytes = taps == 27 ? Halo<27>::A_BYTES : Halo<1>::A_BYTES;
-    const int stage = a_bytes + 2 * taps * a.nt * 16;
+    const long long grid = (long long)a.tiles_w * a.tiles_h * a.tiles_d * L.n * a.ntiles;
+    if (grid <= 0) return FSIM_OK;
+    const int nchunk = L.cin / 16;
+    if (taps == 27) {
+        if (grid >= (1ll << 31)) return FSIM_E_INVALID;
+        PersArgs p{};
+        const int A = Halo<27>::A_BYTES, B_KC = 27 * a.nt * 16, w_all = nchunk * 2 * B_KC;
+        p.total_tiles = (int)grid;
+        p.ncols = tmem_cols(TD * a.nt);
+        if (2 * p.ncols > 512) return FSIM_E_INVALID;
+        const int room = SMEM_LIMIT - 128;
+        if (a.ntiles == 1 && w_all + 2 * A <= room) {
+            p.wres = 1;
+            p.stage_bytes = A;
+            a.stages = (room - w_all) / A;
+        } else {
+            p.wres = 0;
+            p.stage_bytes = A + 2 * B_KC;
+            a.stages = room / p.stage_bytes;
+        }
+        if (a.stages < 2) return FSIM_E_INVALID;
+        if (a.stages > PERS_MAX_STAGES) a.stages = PERS_MAX_STAGES;
+        p.m = a;
+        int smem = a.stages * p.stage_bytes + (p.wres ? w_all : 0) + 128;
+        if (smem < SMEM_LIMIT / 2 + 1024) smem = SMEM_LIMIT / 2 + 1024;  // one CTA per SM
+        static int sms[64] = {0};
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return FSIM_E_CUDA;
+        if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return FSIM_E_CUDA;
+        const int ctas = grid < sms[dev] ? (int)grid : sms[dev];
+        if (set_smem_limit((const void*)k_conv_pers, SMEM_LIMIT) != cudaSuccess) return FSIM_E_CUDA;
+        k_conv_pers<<<ctas, PERS_THREADS, smem, s>>>(p, *L.mx, *L.mw);
+        return cudaGetLastError() == cudaSuccess ? FSIM_OK : FSIM_E_CUDA;
+    }
+    const int a_bytes = Halo<1>::A_BYTES;
+    const int stage = a_bytes + 2 * a.nt * 16;
     if (stage + 128 > SMEM_LIMIT) return FSIM_E_INVALID;
     // as many pipeline stages (<= 3, <= chunks) as keep two CTAs on an SM: the
     // second CTA's loads and epilogue overlap the first one's MMAs
-    const int nchunk = L.cin / 16;
     int stages = 1;
     while (stages < 3 && stages < nchunk && (stages + 1) * stage + 128 <= SMEM_LIMIT / 2) stages++;
     a.stages = stages;
     int smem = stages * stage + 128;
     // the pointwise kernel's accumulator can take all of TMEM: one CTA per SM
-    if (taps == 1 && smem < 160 * 1024) smem = 160 * 1024;
-    const long long grid = (long long)a.tiles_w * a.tiles_h * a.tiles_d * L.n * a.ntiles;
-    if (grid <= 0) return FSIM_OK;
-    if (taps == 27) {
-        if (set_smem_limit((const void*)k_conv_mma<27>, SMEM_LIMIT) != cudaSuccess) return FSIM_E_CUDA;
-        k_conv_mma<27><<<(unsigned)grid, CONV_THREADS, smem, s>>>(a, *L.mx, *L.mw);
-    } else {
-        if (set_smem_limit((const void*)k_conv_mma<1>, SMEM_LIMIT) != cudaSuccess) return FSIM_E_CUDA;
-        k_conv_mma<1><<<(unsigned)grid, CONV_THREADS, smem, s>>>(a, *L.mx, *L.mw);
-    }
+    if (smem < 160 * 1024) smem = 160 * 1024;
+    if (set_smem_limit((const void*)k_conv_mma<1>, SMEM_LIMIT) != cudaSuccess) return FSIM_E_CUDA;
+    k_conv_mma<1><<<(unsigned)grid, CONV_THREADS, smem, s>>>(a, *L.mx, *L.mw);
     return cudaGetLastError() == cudaSuccess ? FSIM_OK : FSIM_E_CUDA;
 }
 

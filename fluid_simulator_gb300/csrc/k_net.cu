@@ -116,34 +116,86 @@ __device__ __forceinline__ void up_src(int f, int nc, int& i0, int& i1, float& l
     l1 = s - (float)i0;
 }
 
-// src: coarse [n][D][H][W][C]; dst: fine, channel stride ds (offset 0)
-__global__ void k_upsample(const bf16* src, int C, int n, int D, int H, int W, bf16* dst, int ds) {
-    const int oct = C / 8;
-    const int FD = 2 * D, FH = 2 * H, FW = 2 * W;
-    const long long total = (long long)n * FD * FH * FW * oct;
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= total) return;
-    const int o = (int)(i % oct);
-    const long long fv = i / oct;
-    const int fw = (int)(fv % FW), fh = (int)((fv / FW) % FH);
-    const long long fdn = fv / ((long long)FW * FH);
-    const int fd = (int)(fdn % FD), nb = (int)(fdn / FD);
-    int d0, d1, h0, h1, w0, w1;
-    float ld, lh, lw;
-    up_src(fd, D, d0, d1, ld);
-    up_src(fh, H, h0, h1, lh);
-    up_src(fw, W, w0, w1, lw);
+// src: coarse [n][D][H][W][C]; dst: fine, channel stride ds (offset 0).
+// One thread per (coarse voxel, 8-channel octet) writes the 2x2x2 fine voxels
+// whose lower trilinear corner lies at or next to it: fine 2k reads coarse
+// k-1 and k, fine 2k+1 reads k and k+1 (clamped at the border).  Per fine
+// (d, h) pair the thread reads the 2 x 2 coarse rows at k-1 and k, writes fine
+// w = 2k, then reads the rows at k+1 and writes w = 2k+1, sharing the samples
+// at k.  The weights and the summation order are those of the per-voxel
+// formula (corner k = (d, h, w) bits, weight = product of the three 1-D
+// weights), so the result does not depend on this blocking.  Coarse indices
+// are 32-bit: the host keeps n * D * H * W * (C / 8) below 2^31.
+__device__ __forceinline__ void up_out(const uint4 (&lo)[4], const uint4 (&hi)[4], bool w0_hi, bool w1_hi, float ld,
+                                       float lh, float lw, bf16* out) {
     float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-        const int dd = (k & 4) ? d1 : d0, hh = (k & 2) ? h1 : h0, ww = (k & 1) ? w1 : w0;
         const float wt = ((k & 4) ? ld : 1.f - ld) * ((k & 2) ? lh : 1.f - lh) * ((k & 1) ? lw : 1.f - lw);
-        float v[8];
-        ld8(src + ((((long long)nb * D + dd) * H + hh) * W + ww) * C + o * 8, v);
+        const int r = ((k & 4) ? 2 : 0) | ((k & 2) ? 1 : 0);
+        const bool use_hi = (k & 1) ? w1_hi : w0_hi;
+        const uint4 u = use_hi ? hi[r] : lo[r];
+        const __nv_bfloat162* hv = reinterpret_cast<const __nv_bfloat162*>(&u);
 #pragma unroll
-        for (int j = 0; j < 8; j++) acc[j] += wt * v[j];
+        for (int j = 0; j < 4; j++) {
+            const float2 f = __bfloat1622float2(hv[j]);
+            acc[2 * j] += wt * f.x;
+            acc[2 * j + 1] += wt * f.y;
+        }
     }
-    st8(dst + fv * ds + o * 8, acc);
+    st8(out, acc);
+}
+
+__global__ void __launch_bounds__(NT_THREADS, 3) k_upsample(const bf16* src, int C, int n, int D, int H, int W,
+                                                            bf16* dst, int ds) {
+    const int oct = C >> 3;
+    const int total = n * D * H * W * oct;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int o = i % oct;
+    int t = i / oct;
+    const int cw = t % W;
+    t /= W;
+    const int chh = t % H;
+    t /= H;
+    const int cd = t % D;
+    const int nb = t / D;
+    const int FD = 2 * D, FH = 2 * H, FW = 2 * W;
+    const int wl = cw > 0 ? cw - 1 : 0, wr = cw < W - 1 ? cw + 1 : cw;
+    // fine w = 2cw reads coarse {i0, i1} in {wl, cw}; fine 2cw + 1 reads them in {cw, wr}
+    int a0, a1, b0, b1;
+    float lwa, lwb;
+    up_src(2 * cw, W, a0, a1, lwa);
+    up_src(2 * cw + 1, W, b0, b1, lwb);
+#pragma unroll 1
+    for (int a = 0; a < 2; a++) {
+        int d0, d1;
+        float ld;
+        up_src(2 * cd + a, D, d0, d1, ld);
+#pragma unroll 1
+        for (int b = 0; b < 2; b++) {
+            int h0, h1;
+            float lh;
+            up_src(2 * chh + b, H, h0, h1, lh);
+            size_t rowb[4];
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                const int dd = (r & 2) ? d1 : d0, hh = (r & 1) ? h1 : h0;
+                rowb[r] = ((size_t)((nb * D + dd) * H + hh) * W) * C + o * 8;
+            }
+            uint4 lo[4], mid[4];
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                lo[r] = *reinterpret_cast<const uint4*>(src + rowb[r] + (size_t)wl * C);
+                mid[r] = *reinterpret_cast<const uint4*>(src + rowb[r] + (size_t)cw * C);
+            }
+            const size_t fv = ((size_t)(nb * FD + 2 * cd + a) * FH + 2 * chh + b) * FW + 2 * cw;
+            up_out(lo, mid, a0 != wl, a1 != wl, ld, lh, lwa, dst + fv * ds + o * 8);
+#pragma unroll
+            for (int r = 0; r < 4; r++) lo[r] = *reinterpret_cast<const uint4*>(src + rowb[r] + (size_t)wr * C);
+            up_out(mid, lo, b0 != cw, b1 != cw, ld, lh, lwb, dst + (fv + 1) * ds + o * 8);
+        }
+    }
 }
 
 // weights of coarse index k in the fine samples near it (adjoint of up_src)
@@ -648,7 +700,8 @@ int upsample(fsim_net* net, int src, int dst) {
     const NetBuf& s = net->act[src];
     const int lv = s.lev;
     const NetShape& sh = net->shape;
-    const long long total = level_vox(sh, lv - 1) * (s.c / 8);
+    const long long total = level_vox(sh, lv) * (s.c / 8);
+    if (total >= (1ll << 31)) return fail(net, "up-sampling volume too large", FSIM_E_CAPACITY);
     k_upsample<<<nblk(total), NT_THREADS, 0, net->stream>>>(s.p, s.c, sh.n, sh.d >> lv, sh.h >> lv, sh.w >> lv,
                                                             net->act[dst].p, net->act[dst].c);
     net->launches++;

@@ -61,7 +61,11 @@ def test_conv_pointwise_forward(gpu):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("shape,cin,cout", [((1, 8, 16, 8), 16, 16), ((2, 6, 10, 12), 48, 32),
-                                            ((1, 8, 16, 16), 128, 64), ((1, 4, 4, 8), 32, 96)])
+                                            ((1, 8, 16, 16), 128, 64), ((1, 4, 4, 8), 32, 96),
+                                            # several tiles per CTA: the stage ring wraps, both TMEM
+                                            # accumulators alternate; resident and streamed weights
+                                            ((2, 64, 64, 64), 16, 16), ((1, 64, 64, 64), 48, 16),
+                                            ((1, 64, 64, 64), 64, 64)])
 def test_conv27_forward(gpu, shape, cin, cout):
     from fluid_simulator_gb300 import native as N
     rng = np.random.default_rng(1)
@@ -75,7 +79,7 @@ def test_conv27_forward(gpu, shape, cin, cout):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("taps,shape,cin,cout", [(27, (2, 6, 10, 12), 16, 32), (27, (1, 8, 16, 8), 48, 16),
-                                                 (1, (1, 8, 8, 8), 256, 64)])
+                                                 (1, (1, 8, 8, 8), 256, 64), (27, (1, 64, 64, 64), 96, 32)])
 def test_conv_input_gradient(gpu, taps, shape, cin, cout):
     from fluid_simulator_gb300 import native as N
     rng = np.random.default_rng(2)
