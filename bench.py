@@ -412,16 +412,20 @@ def drift_dam32(N, every=5):
     O.build_port()
     res, dt, steps = 32, 1.0 / 120.0, 100
     pos = dam_break(GridSpec(res), seed=0)
-    p = N.default_params(transfer=N.FLIP, resolution=res, tol=1e-6, tol_mode=N.TOL_ABS_MAX, max_iters=200)
+    p = N.default_params(transfer=N.FLIP, resolution=res, tol=1e-6, tol_mode=N.TOL_ABS_MAX, max_iters=200,
+                         timing=True)
     sim = N.Simulation(res, p, track_ids=True)
     sim.set_particles(pos)
     o = O.Oracle(O.make_params(res, transfer=O.FLIP, tol=1e-6, max_iters=200), pos.astype(np.float64), lib="port")
-    o.set_threads(os.cpu_count() or 1)
+    threads = os.cpu_count() or 1
+    o.set_threads(threads)
     h = sim.h
-    rows = []
+    rows, gpu_ms, cpu_s = [], [], []
     for _ in range(steps):
-        sim.step(dt)
+        gpu_ms.append(sim.step(dt).ms_total)
+        t0 = time.perf_counter()
         o.step(dt)
+        cpu_s.append(time.perf_counter() - t0)
         gs, gp, gv = _traj_stats(sim, N)
         op, ov, _ = o.particles()
         ke_o = 0.5 * float((ov * ov).sum(axis=1).mean())
@@ -434,7 +438,11 @@ def drift_dam32(N, every=5):
     sim.close()
     o.close()
     r = np.array(rows)
+    # step rates after 3 warm-up steps: the library's CUDA-event step time, the oracle's wall time
+    g_ms, c_s = float(np.median(gpu_ms[3:])), float(np.median(cpu_s[3:]))
     return {"workload": "dam32_flip (32^3, FLIP 0.95, dt 1/120, 51840 particles)", "steps": steps,
+            "gpu_steps_per_s": round(1e3 / g_ms, 1), "gpu_ms_per_step": round(g_ms, 3),
+            "cpu_port_steps_per_s": round(1.0 / c_s, 2), "cpu_port_threads": threads,
             "sampled_every": every, "position_rms_cells": _curve(r[:, 0], every),
             "position_max_cells": _curve(r[:, 1], every), "velocity_rms_rel": _curve(r[:, 2], every),
             "kinetic_energy_rel": _curve(r[:, 3], every), "fluid_cells_diff": [int(x) for x in r[every - 1::every, 4]]}
@@ -474,13 +482,15 @@ def drift_dam128(N, every=10):
                 "tracked_velocity_rms_rel": [float(f"{x:.3g}") for x in dvel]}
 
     for name, transfer in (("pic", N.PIC), ("flip", N.FLIP), ("apic", N.APIC)):
-        p = N.default_params(transfer=transfer, resolution=res, tol=1e-6, tol_mode=N.TOL_ABS_MAX, max_iters=200)
+        p = N.default_params(transfer=transfer, resolution=res, tol=1e-6, tol_mode=N.TOL_ABS_MAX, max_iters=200,
+                             timing=True)
         sim = N.Simulation(res, p, track_ids=True)
         sim.set_particles(pos)
-        stats, tp, tv, its = [], [], [], []
+        stats, tp, tv, its, ms = [], [], [], [], []
         for s in range(1, steps + 1):
             st = sim.step(dt)
             its.append(st.pcg_iterations)
+            ms.append(st.ms_total)
             row, pp, vv = _traj_stats(sim, N)
             stats.append(row)
             if s % sample == 0:
@@ -489,9 +499,27 @@ def drift_dam128(N, every=10):
         sim.close()
         out[name] = compare(np.array(stats), np.array(tp), np.array(tv), name)
         out[name]["gpu_pcg_iterations_mean"] = round(float(np.mean(its)), 2)
+        g_ms = float(np.median(ms[3:]))
+        out[name]["gpu_steps_per_s"] = round(1e3 / g_ms, 1)
+        out[name]["gpu_particle_steps_per_s"] = round(pos.shape[0] * 1e3 / g_ms, 1)
         out[name]["oracle_pcg_iterations_mean"] = round(float(gold[f"{name}_stats"][:, 6].mean()), 2)
     ref = gold["flip_threads8_stats"]
     out["fp64_threads"] = compare(ref, gold["flip_threads8_pos"], gold["flip_threads8_vel"], "flip")
+    # CPU side of the same workload: the oracle (APIC, all host threads), 2 timed steps after 1
+    from oracle import oracle as O
+
+    O.build_port()
+    o = O.Oracle(O.make_params(res, transfer=O.APIC, tol=1e-6, max_iters=200), pos.astype(np.float64), lib="port")
+    threads = os.cpu_count() or 1
+    o.set_threads(threads)
+    o.step(dt)
+    t0 = time.perf_counter()
+    for _ in range(2):
+        o.step(dt)
+    c_s = (time.perf_counter() - t0) / 2
+    o.close()
+    out["cpu_port_apic"] = {"steps_per_s": round(1.0 / c_s, 3), "threads": threads,
+                            "sample": "2 steps after 1 of the APIC dam break from the seeded start"}
     return out
 
 

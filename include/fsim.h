@@ -385,9 +385,11 @@ int fsim_p2g_noalloc(const fsim_grid_desc *grid, int transfer, const float *pos,
  * right-hand side and cell types to a pressure guess.  BF16 weights and
  * activations, FP32 accumulation on the tensor cores, FP32 master parameters
  * trained with Adam.  The guess only seeds PCG: with params.warm_start ==
- * FSIM_WARM_LEARNED the solver compares its residual with that of the previous
- * step's pressure, starts from the better one and iterates to the same
- * tolerance.
+ * FSIM_WARM_LEARNED (the network's pressure) or FSIM_WARM_LEARNED_RESIDUAL (the
+ * previous step's pressure plus the network's answer to the residual that
+ * pressure leaves) the solver compares the guess's residual with that of the
+ * previous step's pressure, starts from the better one and iterates to the
+ * same tolerance.
  *
  * Network input: [n][d][h][w][4] FP32 = (rhs / rms(rhs over fluid cells),
  * fluid, solid, air); output [n][d][h][w] FP32 = pressure / rms(rhs), both in
