@@ -97,9 +97,10 @@ class ProblemSolver:
         self.sim = N.Simulation(n, self.params)
         self.dt = 1.0 / float(n * n)  # rho h^2 with rho = 1, h = 1/n: scale 1
 
-    def solve(self, flags, rhs, *, warm: int = N.WARM_ZERO, tol: float | None = None, backoff: bool = False):
+    def solve(self, flags, rhs, *, warm: int = N.WARM_ZERO, tol: float | None = None, backoff: bool = False,
+              precond: int = N.PRECOND_MG):
         p = N.default_params(resolution=self.n, tol=self.tol if tol is None else tol, tol_mode=N.TOL_REL_L2,
-                             max_iters=4000, warm_start=warm, timing=True, learned_backoff=backoff)
+                             max_iters=4000, warm_start=warm, timing=True, learned_backoff=backoff, precond=precond)
         self.sim.set_params(p)
         self.sim.set_grid(N.F_FLAGS, flags)
         self.sim.set_grid(N.F_PRESSURE, np.zeros(flags.shape, np.float32))
