@@ -68,56 +68,78 @@ def obstacles_at(t: float, dt: float, h: float, N):
 
 # ---------------------------------------------------------------- helpers
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 50 ms from before the
+    warm-up steps to the end of the timed region; each sample carries its
+    timestamp, so the summary can tell the timed window from the rest of the
+    loaded period."""
 
     def __init__(self, path: str, gpu: int):
         self.path = path
         self.proc = None
         self.gpu = gpu
+        self.t_load = self.t0 = self.t1 = None
 
     def __enter__(self):
-        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+        time.sleep(0.3)  # let the first samples come before the load starts
+        self.t_load = time.time()
         return self
+
+    def timed(self, start: bool):
+        if start:
+            self.t0 = time.time()
+        else:
+            self.t1 = time.time()
 
     def __exit__(self, *exc):
         if self.proc is not None:
-            self.proc.terminate()
+            import signal
+
+            time.sleep(0.1)
+            self.proc.send_signal(signal.SIGINT)  # nvidia-smi ends its loop and flushes
             try:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
+                self.proc.wait()
             self.f.close()
 
     def summary(self):
         if self.proc is None or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm, smax, reasons = [], [], set()
+        import datetime
+
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(parts[2]), float(parts[3]),
+                             {nm for nm, val in zip(names, parts[6:10]) if val.lower() == "active"}))
             except ValueError:
                 continue
-            for nm, val in zip(names, parts[5:9]):
-                if val.lower() == "active":
-                    reasons.add(nm)
-        if not sm:
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        t_end = self.t1 if self.t1 is not None else rows[-1][0]
+        timed = [r for r in rows if self.t0 is not None and self.t0 <= r[0] <= t_end]
+        loaded = [r for r in rows if self.t_load is not None and self.t_load <= r[0] <= t_end] or rows
+        use = timed if len(timed) >= 3 else loaded
+        return {"sm_mhz": statistics.median(r[1] for r in use), "sm_max_mhz": max(r[2] for r in use),
+                "reasons": sorted(set().union(*(r[3] for r in use))),
+                "samples": len(use), "samples_timed": len(timed),
+                "window": "timed region" if use is timed else "warm-up and timed steps"}
 
 
 def load_peaks():
@@ -231,18 +253,21 @@ def run_fsim(args):
         t += dt
         return st
 
-    for _ in range(args.warmup):
-        step()
-    stream = sim.lib.fsim_stream(sim.ctx)
-    ev = Events(rt, stream)
-    stats = []
-    barrier(dist)
-    sim.synchronize()
-    with ClockSampler(os.path.join(args.out_dir, f"clocks_rank{rank}.csv"), local) as clk:
+    clk = ClockSampler(os.path.join(args.out_dir, f"clocks_rank{rank}.csv"), local)
+    with clk:
+        for _ in range(args.warmup):
+            step()
+        stream = sim.lib.fsim_stream(sim.ctx)
+        ev = Events(rt, stream)
+        stats = []
+        barrier(dist)
+        sim.synchronize()
+        clk.timed(True)
         ev.start()
         for _ in range(args.steps):
             stats.append(step())
         ms = ev.stop_ms()
+        clk.timed(False)
     sim.synchronize()
     barrier(dist)
     ms_max = dist_max(dist, ms)
