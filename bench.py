@@ -278,8 +278,12 @@ def run_fsim(args):
     # land in host memory while the next step runs; the timed region ends after
     # the last copy (fsim_gfx_wait)
     n_cap = int(sim.n * 1.2) + 1_000_000
-    gfx = (N.ParticleGfx * n_cap)()
-    rt.cudaHostRegister(C.cast(gfx, C.c_void_p), C.c_size_t(C.sizeof(gfx)), 0)
+    # pinned host memory from the CUDA allocator (a registered ctypes array made
+    # the copy rate vary from run to run with the host's page layout)
+    gfx_ptr = C.c_void_p()
+    if rt.cudaHostAlloc(C.byref(gfx_ptr), C.c_size_t(n_cap * C.sizeof(N.ParticleGfx)), 0) != 0:
+        raise RuntimeError("cudaHostAlloc of the gfx buffer failed")
+    gfx = (N.ParticleGfx * n_cap).from_address(gfx_ptr.value)
     # every copy is inside the window; the last one is waited for at its end, so
     # longer windows measure the steady state (the tail is one copy, ~7 ms)
     e2e_steps = max(1, min(args.steps, 20))
@@ -323,7 +327,8 @@ def run_fsim(args):
         pub.append(time.perf_counter() - t0)
     pub_s = min(pub)
     pub_bytes = got.value * C.sizeof(N.ParticleGfx)
-    rt.cudaHostUnregister(C.cast(gfx, C.c_void_p))
+    del gfx
+    rt.cudaFreeHost(gfx_ptr)
 
     # per-stage breakdown (library events)
     def mean(key):
