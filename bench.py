@@ -240,7 +240,7 @@ def run_fsim(args):
                          spawning=True, despawning=True, timing=True, precision=N.PREC_MIXED,
                          warm_start=N.WARM_ZERO, precond=precond, mg_sweeps=args.mg_sweeps,
                          mg_coarse_sweeps=args.mg_coarse_sweeps, mg_cluster_sweeps=args.mg_cluster_sweeps,
-                         refine_digits=args.refine_digits)
+                         refine_digits=args.refine_digits, mg_boundary_sweeps=args.mg_boundary_sweeps)
     sim = N.Simulation(res, p)
     sim.set_particles(pos)
     del pos
@@ -875,6 +875,8 @@ def main():
                     help="multigrid smoothing sweeps before and after the coarse correction (0: library default)")
     ap.add_argument("--mg-coarse-sweeps", type=int, default=0,
                     help="multigrid sweeps on the coarser levels (0: as --mg-sweeps)")
+    ap.add_argument("--mg-boundary-sweeps", type=int, default=0,
+                    help="extra red-black sweeps on the finest level's free-surface band (0: 3, -1: none)")
     ap.add_argument("--mg-cluster-sweeps", type=int, default=0,
                     help="multigrid sweeps on the levels run by the cluster kernel (0: library default)")
     ap.add_argument("--precision-study", type=int, default=1,

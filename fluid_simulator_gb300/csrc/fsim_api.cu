@@ -387,6 +387,7 @@ int validate_params(const fsim_params* p, std::string& why) {
         why = "warm_start";
         return FSIM_E_INVALID;
     }
+    if (p->mg_boundary_sweeps < -1 || p->mg_boundary_sweeps > 8) { why = "mg_boundary_sweeps"; return FSIM_E_INVALID; }
     return FSIM_OK;
 }
 

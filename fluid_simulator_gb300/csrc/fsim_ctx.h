@@ -70,6 +70,8 @@ struct SolverBufs {
     double last_scale = 1.0;      // dt / (rho h^2) of the last solve
     std::vector<MGLevelBufs> mg;  // multigrid hierarchy (built at allocation)
     int mg_cluster = 0;           // CTAs in the coarse-V-cycle cluster (0: separate launches)
+    int4* bnd_quads = nullptr;    // finest-level quads of the free-surface band {x, y, z0, 0}
+    int* d_nbnd = nullptr;        // their count (device)
     // one PCG iteration as a CUDA graph, captured on first use per configuration
     // (precision, preconditioner, sweep counts); up to four are kept
     static constexpr int kIterGraphs = 4;
