@@ -876,7 +876,8 @@ def main():
     ap.add_argument("--mg-coarse-sweeps", type=int, default=0,
                     help="multigrid sweeps on the coarser levels (0: as --mg-sweeps)")
     ap.add_argument("--mg-boundary-sweeps", type=int, default=0,
-                    help="extra red-black sweeps on the finest level's free-surface band (0: 3, -1: none)")
+                    help="extra red-black sweeps on the finest level's free-surface band "
+                         "(0: 3 on grids of 2^23 cells or more, else none; -1: none)")
     ap.add_argument("--mg-cluster-sweeps", type=int, default=0,
                     help="multigrid sweeps on the levels run by the cluster kernel (0: library default)")
     ap.add_argument("--precision-study", type=int, default=1,

@@ -550,9 +550,14 @@ constexpr int MIXED_REFINE_DIGITS = 3;
 // sweeps / band sweeps): 2/0 46.8 (17.2 iterations), 1/0 47.8 (19.4), 1/2
 // 48.7 (17.8), 1/3 49.3 (17.1), 1/4 49.0 (17.0), 1/5 48.6, 2/4 46.9 (16.0),
 // 2/6 45.8: one full sweep plus three band sweeps recover the iterations a
-// second full sweep saved, for about a third of its cost.
-constexpr int MG_NU_DEFAULT = 1;           // level 0
-constexpr int MG_NB_DEFAULT = 3;           // level 0 free-surface band
+// second full sweep saved, for about a third of its cost.  On smaller grids the
+// band's launches cost more than the full sweep they replace (128^3 dam break:
+// 173 -> 158 steps/s, 32^3: 480 -> 399), so the band is the default only from
+// MG_BAND_MIN_CELLS cells on.
+constexpr long long MG_BAND_MIN_CELLS = 1ll << 23;
+constexpr int MG_NU_DEFAULT_BIG = 1;       // level 0, grids of MG_BAND_MIN_CELLS cells or more
+constexpr int MG_NB_DEFAULT_BIG = 3;       // level 0 free-surface band, same grids
+constexpr int MG_NU_DEFAULT = 2;           // level 0, smaller grids (no band)
 constexpr int MG_NU_L1_DEFAULT = 4;        // level 1 (128^3 at 256^3)
 constexpr int MG_NU_COARSE_DEFAULT = 6;    // deeper separately launched levels
 constexpr int MG_NU_CLUSTER_DEFAULT = 8;   // cluster levels in global or distributed shared memory
@@ -1849,13 +1854,21 @@ static void mg_setup(fsim_ctx* ctx) {
     }
 }
 
+// free-surface band sweeps on level l (only the finest level has a band)
+static int mg_band_sweeps(const SolverBufs& S, const fsim_params& P, int l) {
+    if (l != 0 || P.mg_boundary_sweeps < 0) return 0;
+    if (P.mg_boundary_sweeps > 0) return P.mg_boundary_sweeps;
+    return S.mg[0].ncell >= MG_BAND_MIN_CELLS ? MG_NB_DEFAULT_BIG : 0;
+}
+
 // z = V-cycle(r); r is the current PCG residual (r0 or r1 by device state).
 // first_fused: the first level-0 sweep was done by k_update; dot_mode >= 0: the
 // last level-0 sweep also computes z.r and the CG scalars (k_red modes).
 static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, const float* r1, float* z,
                       bool first_fused, int dot_mode) {
     const fsim_params& P = ctx->prm;
-    const int NU0 = P.mg_sweeps > 0 ? P.mg_sweeps : MG_NU_DEFAULT;
+    const bool big = ctx->sv.mg[0].ncell >= MG_BAND_MIN_CELLS;
+    const int NU0 = P.mg_sweeps > 0 ? P.mg_sweeps : (big ? MG_NU_DEFAULT_BIG : MG_NU_DEFAULT);
     const int NU1 = P.mg_coarse_sweeps > 0 ? P.mg_coarse_sweeps : MG_NU_COARSE_DEFAULT;
     const int NUC = P.mg_cluster_sweeps > 0 ? P.mg_cluster_sweeps : MG_NU_CLUSTER_DEFAULT;
     const int NU = l == 0 ? NU0 : (P.mg_coarse_sweeps > 0 ? NU1 : (l == 1 ? MG_NU_L1_DEFAULT : NU1));
@@ -1933,8 +1946,7 @@ static void mg_vcycle(fsim_ctx* ctx, const PcgArgs& A, int l, const float* r0, c
         smooth(1, 0);
         ctx->launches += 2;
     }
-    const int NB = l != 0 || P.mg_boundary_sweeps < 0 ? 0 : (P.mg_boundary_sweeps > 0 ? P.mg_boundary_sweeps
-                                                                                      : MG_NB_DEFAULT);
+    const int NB = mg_band_sweeps(S, P, l);
     auto smooth_band = [&](int color) {
         launch_pdl(k_mg_smooth_bnd, G, PCG_THREADS, st, A, L, (const int4*)S.bnd_quads, (const int*)S.d_nbnd, color);
         ctx->launches += 1;
@@ -2097,7 +2109,7 @@ static int run_pcg(fsim_ctx* ctx, PcgArgs& A, Vecs<T> v, int precision, int prec
         }
     };
     if (mg) mg_setup(ctx);
-    if (mg && ctx->prm.mg_boundary_sweeps >= 0) {
+    if (mg && mg_band_sweeps(S, ctx->prm, 0) > 0) {
         if (!S.bnd_quads) {
             FSIM_CUDA_TRY(ctx, cudaMalloc(&S.bnd_quads, (size_t)(ctx->g.ncell / 4 + 1) * sizeof(int4)));
             FSIM_CUDA_TRY(ctx, cudaMalloc(&S.d_nbnd, sizeof(int)));

@@ -172,7 +172,7 @@ typedef struct fsim_params {
     int timing;             /* record per-stage CUDA-event times into fsim_step_stats */
     int precond;            /* fsim_precond (FSIM_PREC_FP64 always uses FSIM_PRECOND_RBIC) */
     int mg_sweeps;          /* multigrid smoothing sweeps before and after the coarse correction on
-                               the finest level (0: 1) */
+                               the finest level (0: 1 on grids of 2^23 cells or more, else 2) */
     int mg_coarse_sweeps;   /* the same on level 1 and other levels run as separate kernels (0: 4 on
                                level 1, 6 below it) */
     int mg_cluster_sweeps;  /* the same on the small levels run by one thread-block cluster (0: 8 on
@@ -186,8 +186,8 @@ typedef struct fsim_params {
                                10^refine_digits (0: 3) */
     int mg_boundary_sweeps; /* extra red-black sweeps on the finest level's free-surface band (quads
                                within one cell of a fluid cell next to air), after the pre-smoothing
-                               and, in reverse order, before the post-smoothing (0: 3; -1: none;
-                               at most 8) */
+                               and, in reverse order, before the post-smoothing (0: 3 on grids of
+                               2^23 cells or more, else none; -1: none; at most 8) */
 } fsim_params;
 
 /* Obstacle (obstacles.hpp:7-65), speed set by the caller as (pos-prevPos)/dt. */
