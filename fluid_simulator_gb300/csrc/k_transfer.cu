@@ -424,35 +424,47 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
                     sg[2][o] = e > 0.0 ? -1.f : 1.f;
                 }
             }
-            // corner weight (wx wy) wz; a gradient term sign * wy * wz / h equals
-            // sign * ((wy wz) / h) exactly (rounding is symmetric in the sign), so the
-            // four magnitudes per component are formed once per axis
-            float wxy[2][2], gmx[2][2], gmy[2][2], gmz[2][2];
+            // The trilinear sums factor by dimension: contract the 2x2x2 corner
+            // values along z, then y, then x, with the 1-D weights w and the signed
+            // gradient factors g = sign / h (trilinearInterpoll and
+            // trilinearInterpollGradient summed over the eight corners, in half
+            // the arithmetic of a corner-by-corner sum).
+            float gx[2], gy[2], gz[2];
 #pragma unroll
-            for (int i2 = 0; i2 < 2; i2++)
+            for (int o = 0; o < 2; o++) {
+                gx[o] = sg[0][o] * hinv;
+                gy[o] = sg[1][o] * hinv;
+                gz[o] = sg[2][o] * hzinv;
+            }
+            float A[2][2], Bz[2][2], Fz[2][2];
 #pragma unroll
-                for (int j2 = 0; j2 < 2; j2++) {
-                    wxy[i2][j2] = w1[0][i2] * w1[1][j2];
-                    if (MODE == 2) {
-                        gmx[i2][j2] = (w1[1][i2] * w1[2][j2]) * hinv;  // (oy, oz)
-                        gmy[i2][j2] = (w1[0][i2] * w1[2][j2]) * hinv;  // (ox, oz)
-                        gmz[i2][j2] = wxy[i2][j2] * hzinv;             // (ox, oy)
-                    }
+            for (int ox = 0; ox < 2; ox++)
+#pragma unroll
+                for (int oy = 0; oy < 2; oy++) {
+                    const int si = ((sx + ox) * BY + (sy + oy)) * BZ + sz;
+                    const float va = sv2[ax * BOXN + si], vb = sv2[ax * BOXN + si + 1];
+                    A[ox][oy] = w1[2][0] * va + w1[2][1] * vb;
+                    if (MODE == 2) Bz[ox][oy] = gz[0] * va + gz[1] * vb;
+                    if (MODE == 1)
+                        Fz[ox][oy] = w1[2][0] * (va - su[ax * BOXN + si]) + w1[2][1] * (vb - su[ax * BOXN + si + 1]);
                 }
-            float pic = 0.f, flip = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
+            float P[2], Gy[2], Q[2], Fy[2];
 #pragma unroll
-            for (int o = 0; o < 8; o++) {
-                const int ox = o >> 2, oy = (o >> 1) & 1, oz = o & 1;
-                const float w = wxy[ox][oy] * w1[2][oz];
-                const int si = ((sx + ox) * BY + (sy + oy)) * BZ + (sz + oz);
-                const float v2 = sv2[ax * BOXN + si];
-                pic += v2 * w;
-                if (MODE == 1) flip += (v2 - su[ax * BOXN + si]) * w;
+            for (int ox = 0; ox < 2; ox++) {
+                P[ox] = w1[1][0] * A[ox][0] + w1[1][1] * A[ox][1];
                 if (MODE == 2) {
-                    c0 += (sg[0][ox] * gmx[oy][oz]) * v2;
-                    c1 += (sg[1][oy] * gmy[ox][oz]) * v2;
-                    c2 += (sg[2][oz] * gmz[ox][oy]) * v2;
+                    Gy[ox] = gy[0] * A[ox][0] + gy[1] * A[ox][1];
+                    Q[ox] = w1[1][0] * Bz[ox][0] + w1[1][1] * Bz[ox][1];
                 }
+                if (MODE == 1) Fy[ox] = w1[1][0] * Fz[ox][0] + w1[1][1] * Fz[ox][1];
+            }
+            const float pic = w1[0][0] * P[0] + w1[0][1] * P[1];
+            float flip = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
+            if (MODE == 1) flip = w1[0][0] * Fy[0] + w1[0][1] * Fy[1];
+            if (MODE == 2) {
+                c0 = gx[0] * P[0] + gx[1] * P[1];
+                c1 = w1[0][0] * Gy[0] + w1[0][1] * Gy[1];
+                c2 = w1[0][0] * Q[0] + w1[0][1] * Q[1];
             }
             if (MODE == 0) vnew[ax] = pic;
             if (MODE == 1) vnew[ax] = pic * a.pic_w + (flip + a.src.v[ax][i]) * a.fr;
