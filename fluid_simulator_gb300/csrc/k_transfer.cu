@@ -338,14 +338,22 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
     if (threadIdx.x >= 32 && threadIdx.x < 64) seg_pre[threadIdx.x + 1] += seg_pre[32];
     __syncthreads();
     const int total = seg_pre[TX * TY];
-    // sorted slot of the tile's j-th particle
+    // sorted slot of the tile's j-th particle: its row by binary search for a
+    // thread's first particle, then by stepping forward from the previous row
+    // (a thread's particles come in increasing j, a row is ~TZ*8 particles)
+    int row = 0;
     auto slot_of = [&](int j) {
         int lo = 0, hi = TX * TY - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
             if (seg_pre[mid] <= j) lo = mid; else hi = mid - 1;
         }
+        row = lo;
         return seg_beg[lo] + (j - seg_pre[lo]);
+    };
+    auto slot_next = [&](int j) {
+        while (row + 1 < TX * TY && seg_pre[row + 1] <= j) row++;
+        return seg_beg[row] + (j - seg_pre[row]);
     };
     // software pipeline: each thread's next particle (slot, index, position) is
     // loaded one iteration ahead; the first one while the grid tile is in flight
@@ -383,7 +391,7 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
         const uint32_t i = in;
         const float px = pn[0], py = pn[1], pz = pn[2];
         if (j + (int)blockDim.x < total) {
-            kn = slot_of(j + blockDim.x);
+            kn = slot_next(j + blockDim.x);
             in = a.perm[kn];
             pn[0] = a.src.p[0][in]; pn[1] = a.src.p[1][in]; pn[2] = a.src.p[2][in];
         }
