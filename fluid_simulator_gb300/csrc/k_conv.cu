@@ -5,10 +5,13 @@
 // BF16 [tap][cout][cin] (tap = (kd*3 + kh)*3 + kw for 3x3x3, a single tap for
 // the pointwise convolutions).  Accumulation is FP32.
 //
-// Forward / input-gradient kernel (k_conv_mma): implicit GEMM
+// Forward / input-gradient kernels: implicit GEMM
 //   D[m, n] = sum_{tap, c} X[voxel(m) + off(tap), c] * W[tap, n, c]
-// One CTA owns an output tile of 8 (w) x 16 (h) x 4 (d) voxels and NT output
-// channels.  Per 16-channel chunk of the input it loads ONE halo box of the
+// over output tiles of 8 (w) x 16 (h) x 4 (d) voxels and NT output channels:
+// k_conv_pers (3x3x3 layers) is persistent, one CTA per SM walking the tiles
+// with warp-specialized roles (described at the kernel); k_conv_mma (the
+// pointwise down-convolutions) gives each CTA one tile.  Per 16-channel chunk
+// of the input a CTA loads ONE halo box of the
 // input (10 x 18 x 6 voxels for 3x3x3, zero-filled outside the volume, which
 // is the padding) and the chunk's weights for all taps with TMA, in the
 // no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core matrix,
