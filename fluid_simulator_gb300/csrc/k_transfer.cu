@@ -54,11 +54,21 @@ struct P2GArgs {
 // tile narrow in x (the slowest axis of the cell order) spans fewer runs of
 // sorted particles, and the smaller shared-memory share leaves L1 more room
 // for the particle re-reads of the four warp roles.
-constexpr int PX = 8, PY = 16, PZ = 16;
-constexpr int QX = PX + 2, QY = PY + 2, QZ = PZ + 2;
-constexpr int PCELLS = PX * PY * PZ;
-constexpr int P2G_SMEM = 7 * PCELLS * (int)sizeof(float);  // 57,344 B
-constexpr int P2G_THREADS = 384;
+template <int X, int Y, int Z, int THREADS, int MINB>
+struct P2GShape {
+    static constexpr int PX = X, PY = Y, PZ = Z, QX = X + 2, QY = Y + 2, QZ = Z + 2;
+    static constexpr int PCELLS = X * Y * Z;
+    static constexpr int SMEM = 7 * PCELLS * (int)sizeof(float);
+    static constexpr int NTHREADS = THREADS, MIN_BLOCKS = MINB;
+};
+// the default: 8x16x16 tiles (57,344 B), three warp quads per CTA, two CTAs per SM
+using P2GFast = P2GShape<8, 16, 16, 384, 2>;
+// bit-reproducible (fsim_params.deterministic): one warp quad per CTA, so each
+// shared accumulator is added to by a single warp in program order (a warp's
+// lanes hold distinct cells: one flush instruction never adds twice to an
+// address); 8x8x16 tiles (28,672 B), six CTAs per SM.  5.9 against 4.6 ms at
+// 256^3 (8x16x16 tiles with one quad: 8.1 ms).
+using P2GDet = P2GShape<8, 8, 16, 128, 6>;
 
 // 1D tent weights of the three cell-centred nodes at relative -0.5, 0.5, 1.5
 // (f = position in the cell, 0 <= f < 1): the two nodes the reference's
@@ -112,10 +122,11 @@ __device__ __forceinline__ void p2g_face_axis(const float (&f)[3], const float (
         }
 }
 
-template <int AX, int OW, int OV, int NA, int TZ = PZ>
+template <int AX, int OW, int OV, int NA, class S>
 __device__ __forceinline__ void p2g_flush_axis(const float (&acc)[NA], int cx, int cy, int cz, int x0, int y0,
                                                int z0, float* s_vw, float* s_w) {
     constexpr int b = AX == 0 ? 1 : 0, c = AX == 2 ? 1 : 2;
+    constexpr int PX = S::PX, PY = S::PY, TZ = S::PZ;
     constexpr int NCELL = PX * PY * TZ;
 #pragma unroll
     for (int e = 0; e < 18; e++) {
@@ -132,8 +143,10 @@ __device__ __forceinline__ void p2g_flush_axis(const float (&acc)[NA], int cx, i
     }
 }
 
-template <bool APIC>
-__global__ void __launch_bounds__(P2G_THREADS, 2) k_p2g(const P2GArgs a) {
+template <bool APIC, class S>
+__global__ void __launch_bounds__(S::NTHREADS, S::MIN_BLOCKS) k_p2g(const P2GArgs a) {
+    constexpr int PX = S::PX, PY = S::PY, PZ = S::PZ, QX = S::QX, QY = S::QY, QZ = S::QZ;
+    constexpr int PCELLS = S::PCELLS, P2G_THREADS = S::NTHREADS;
     extern __shared__ float sm[];
     float* s_vw = sm;                // [3][PCELLS]
     float* s_w = sm + 3 * PCELLS;   // [3][PCELLS]
@@ -211,11 +224,11 @@ __global__ void __launch_bounds__(P2G_THREADS, 2) k_p2g(const P2GArgs a) {
                 atomicAdd(&s_avg[(lx * PY + ly) * PZ + lz], acc[e]);
             }
         } else if (role == 0) {
-            p2g_flush_axis<0, 0, 18, 36, PZ>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
+            p2g_flush_axis<0, 0, 18, 36, S>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
         } else if (role == 1) {
-            p2g_flush_axis<1, 0, 18, 36, PZ>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
+            p2g_flush_axis<1, 0, 18, 36, S>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
         } else {
-            p2g_flush_axis<2, 0, 18, 36, PZ>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
+            p2g_flush_axis<2, 0, 18, 36, S>(acc, cx, cy, cz, x0, y0, z0, s_vw, s_w);
         }
     }
     __syncthreads();
@@ -509,31 +522,40 @@ __global__ void __launch_bounds__(G2P_THREADS) k_g2p(const G2PArgs a, const __gr
 
 }  // namespace
 
+namespace {
+template <class S>
+cudaError_t launch_p2g_shape(P2GArgs a, bool apic, cudaStream_t stream) {
+    a.ntx = ceil_div(a.g.nx, S::PX);
+    a.nty = ceil_div(a.g.ny, S::PY);
+    a.ntz = ceil_div(a.g.nz, S::PZ);
+    const int nb = a.ntx * a.nty * a.ntz;
+    cudaError_t e = set_smem_limit((const void*)(apic ? k_p2g<true, S> : k_p2g<false, S>), S::SMEM);
+    if (e != cudaSuccess) return e;
+    if (apic)
+        k_p2g<true, S><<<nb, S::NTHREADS, S::SMEM, stream>>>(a);
+    else
+        k_p2g<false, S><<<nb, S::NTHREADS, S::SMEM, stream>>>(a);
+    return cudaGetLastError();
+}
+}  // namespace
+
 void launch_p2g(fsim_ctx* ctx) {
-    const GridGeom& g = ctx->g;
     P2GArgs a;
     a.p = ctx->buf[ctx->cur];
     a.perm = ctx->perm;
     a.cstart = ctx->cstart;
-    a.g = g;
+    a.g = ctx->g;
     for (int k = 0; k < 3; k++) a.u[k] = ctx->u[k];
     a.flags = ctx->flags;
     a.avg = ctx->avg;
-    a.ntx = ceil_div(g.nx, PX);
-    a.nty = ceil_div(g.ny, PY);
-    a.ntz = ceil_div(g.nz, PZ);
-    const int nb = a.ntx * a.nty * a.ntz;
     ctx->launches += 1;
-    set_smem_limit((const void*)k_p2g<false>, P2G_SMEM);
-    set_smem_limit((const void*)k_p2g<true>, P2G_SMEM);
-    if (ctx->prm.transfer == FSIM_APIC)
-        k_p2g<true><<<nb, P2G_THREADS, P2G_SMEM, ctx->stream>>>(a);
-    else
-        k_p2g<false><<<nb, P2G_THREADS, P2G_SMEM, ctx->stream>>>(a);
+    const bool apic = ctx->prm.transfer == FSIM_APIC;
+    if (ctx->prm.deterministic) launch_p2g_shape<P2GDet>(a, apic, ctx->stream);
+    else launch_p2g_shape<P2GFast>(a, apic, ctx->stream);
 }
 
 // P2G on caller-provided buffers (used by the allocation-free entry point in
-// fsim_static.cu); same kernel as launch_p2g.
+// fsim_static.cu); the default kernel of launch_p2g.
 cudaError_t launch_p2g_raw(ParticleBuf p, const uint32_t* perm, const int* cstart, const GridGeom& g,
                            float* const u[3], uint8_t* flags, float* avg, bool apic, cudaStream_t stream) {
     P2GArgs a;
@@ -544,17 +566,7 @@ cudaError_t launch_p2g_raw(ParticleBuf p, const uint32_t* perm, const int* cstar
     for (int k = 0; k < 3; k++) a.u[k] = u[k];
     a.flags = flags;
     a.avg = avg;
-    a.ntx = ceil_div(g.nx, PX);
-    a.nty = ceil_div(g.ny, PY);
-    a.ntz = ceil_div(g.nz, PZ);
-    const int nb = a.ntx * a.nty * a.ntz;
-    cudaError_t e = set_smem_limit((const void*)(apic ? k_p2g<true> : k_p2g<false>), P2G_SMEM);
-    if (e != cudaSuccess) return e;
-    if (apic)
-        k_p2g<true><<<nb, P2G_THREADS, P2G_SMEM, stream>>>(a);
-    else
-        k_p2g<false><<<nb, P2G_THREADS, P2G_SMEM, stream>>>(a);
-    return cudaGetLastError();
+    return launch_p2g_shape<P2GFast>(a, apic, stream);
 }
 
 // TMA descriptors of the six face arrays (v2 x/y/z, v x/y/z): 3D tensors

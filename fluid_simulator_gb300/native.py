@@ -49,7 +49,7 @@ class Params(C.Structure):
         ("warm_start", C.c_int), ("track_ids", C.c_int), ("timing", C.c_int), ("precond", C.c_int),
         ("mg_sweeps", C.c_int), ("mg_coarse_sweeps", C.c_int), ("mg_cluster_sweeps", C.c_int),
         ("grid_solver", C.c_int), ("learned_backoff", C.c_int), ("refine_digits", C.c_int),
-        ("mg_boundary_sweeps", C.c_int),
+        ("mg_boundary_sweeps", C.c_int), ("deterministic", C.c_int),
     ]
 
 
@@ -211,7 +211,7 @@ def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: 
                    fluid_density: float = 1.0, timing: bool = False, precond: int = PRECOND_MG,
                    mg_sweeps: int = 0, mg_coarse_sweeps: int = 0, mg_cluster_sweeps: int = 0,
                    grid_solver: int = SOLVER_PCG, push_apart: bool = False, learned_backoff: bool = False,
-                   refine_digits: int = 0, mg_boundary_sweeps: int = 0) -> Params:
+                   refine_digits: int = 0, mg_boundary_sweeps: int = 0, deterministic: bool = False) -> Params:
     """Parameters of the dam-break workloads (reference parameter names in fsim.h)."""
     p = Params()
     p.transfer = transfer
@@ -244,6 +244,7 @@ def default_params(*, transfer: int = FLIP, resolution: float = 32, flip_ratio: 
     p.learned_backoff = int(learned_backoff)
     p.refine_digits = refine_digits
     p.mg_boundary_sweeps = mg_boundary_sweeps
+    p.deterministic = int(deterministic)
     return p
 
 

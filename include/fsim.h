@@ -188,6 +188,10 @@ typedef struct fsim_params {
                                within one cell of a fluid cell next to air), after the pre-smoothing
                                and, in reverse order, before the post-smoothing (0: 3 on grids of
                                2^23 cells or more, else none; -1: none; at most 8) */
+    int deterministic;      /* 1: bit-reproducible steps (same inputs, same bits on every run):
+                               P2G adds into its shared accumulators in one fixed order (one warp
+                               per accumulator, smaller tiles; P2G about 1.3x slower).  Every other
+                               stage is reproducible in either mode. */
 } fsim_params;
 
 /* Obstacle (obstacles.hpp:7-65), speed set by the caller as (pos-prevPos)/dt. */
