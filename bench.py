@@ -409,15 +409,17 @@ def run_fsim(args):
         line["render"] = render_study(sim, N, h, peak)
     sim.close()
     if args.parity and rank == 0 and world == 1:
-        line["parity_drift"] = {"dam32_flip_vs_live_oracle": drift_dam32(N), "dam128_vs_oracle_fixture": drift_dam128(N)}
+        line["parity_drift"] = {"dam32_flip_vs_oracle_fixture": drift_dam32(N), "dam128_vs_oracle_fixture": drift_dam128(N)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(res, dt)
+        line["cpu_baseline"]["configs"] = cpu_baseline_configs()
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------- drift curves
 DRIFT_GOLDEN = os.path.join(ROOT, "tests", "golden", "drift_dam128.npz")
+DRIFT32_GOLDEN = os.path.join(ROOT, "tests", "golden", "drift_dam32.npz")
 
 
 def _traj_stats(sim, N):
@@ -434,48 +436,47 @@ def _curve(a, every):
 
 
 def drift_dam32(N, every=5):
-    """32^3 FLIP dam break (dt 1/120, 100 steps), free-running on both sides from
-    the same seeded particles: the GPU and the oracle (FP64, all host threads)."""
+    """32^3 FLIP dam break (dt 1/120, 100 steps) on the GPU against the oracle's
+    free-running trajectory in tests/golden/drift_dam32.npz (single-threaded FP64
+    oracle = the reference's results; generated by tests/golden/make_drift.py),
+    with the GPU's step rate (library CUDA-event step time after 3 warm-up steps)."""
     from fluid_simulator_gb300.scenes import GridSpec, dam_break
-    from oracle import oracle as O
 
-    O.build_port()
-    res, dt, steps = 32, 1.0 / 120.0, 100
+    if not os.path.exists(DRIFT32_GOLDEN):
+        return {"unavailable": "tests/golden/drift_dam32.npz missing"}
+    gold = np.load(DRIFT32_GOLDEN)
+    res, dt, steps, sample = 32, float(gold["dt"]), int(gold["steps"]), int(gold["sample_every"])
+    tracked = gold["tracked"]
     pos = dam_break(GridSpec(res), seed=0)
     p = N.default_params(transfer=N.FLIP, resolution=res, tol=1e-6, tol_mode=N.TOL_ABS_MAX, max_iters=200,
                          timing=True)
     sim = N.Simulation(res, p, track_ids=True)
     sim.set_particles(pos)
-    o = O.Oracle(O.make_params(res, transfer=O.FLIP, tol=1e-6, max_iters=200), pos.astype(np.float64), lib="port")
-    threads = os.cpu_count() or 1
-    o.set_threads(threads)
     h = sim.h
-    rows, gpu_ms, cpu_s = [], [], []
-    for _ in range(steps):
+    stats, tp, tv, gpu_ms = [], [], [], []
+    for s_ in range(1, steps + 1):
         gpu_ms.append(sim.step(dt).ms_total)
-        t0 = time.perf_counter()
-        o.step(dt)
-        cpu_s.append(time.perf_counter() - t0)
-        gs, gp, gv = _traj_stats(sim, N)
-        op, ov, _ = o.particles()
-        ke_o = 0.5 * float((ov * ov).sum(axis=1).mean())
-        vs = max(float(np.sqrt((ov * ov).sum(axis=1)).max()), 1e-9)
-        dp = np.sqrt(((gp.astype(np.float64) - op) ** 2).sum(axis=1)) / h
-        rows.append((float(np.sqrt((dp * dp).mean())), float(dp.max()),
-                     float(np.sqrt(((gv.astype(np.float64) - ov) ** 2).sum(axis=1).mean())) / vs,
-                     abs(gs[1] - ke_o) / max(ke_o, 1e-12),
-                     int(gs[0]) - int((o.grid(O.F_FLAGS) == O.WATER).sum())))
+        row, pp, vv = _traj_stats(sim, N)
+        stats.append(row)
+        if s_ % sample == 0:
+            tp.append(pp[tracked])
+            tv.append(vv[tracked])
     sim.close()
-    o.close()
-    r = np.array(rows)
-    # step rates after 3 warm-up steps: the library's CUDA-event step time, the oracle's wall time
-    g_ms, c_s = float(np.median(gpu_ms[3:])), float(np.median(cpu_s[3:]))
+    stats, tp, tv = np.array(stats), np.array(tp), np.array(tv)
+    rs, rp, rv = gold["flip_stats"], gold["flip_pos"], gold["flip_vel"]
+    dpos = np.sqrt(((tp.astype(np.float64) - rp) ** 2).sum(axis=2)) / h
+    vs = np.maximum(np.sqrt((rv.astype(np.float64) ** 2).sum(axis=2)).max(axis=1), 1e-9)
+    dvel = np.sqrt(((tv.astype(np.float64) - rv) ** 2).sum(axis=2).mean(axis=1)) / vs
+    ke = np.abs(stats[:, 1] - rs[:, 1]) / np.maximum(rs[:, 1], 1e-12)
+    g_ms = float(np.median(gpu_ms[3:]))
     return {"workload": "dam32_flip (32^3, FLIP 0.95, dt 1/120, 51840 particles)", "steps": steps,
             "gpu_steps_per_s": round(1e3 / g_ms, 1), "gpu_ms_per_step": round(g_ms, 3),
-            "cpu_port_steps_per_s": round(1.0 / c_s, 2), "cpu_port_threads": threads,
-            "sampled_every": every, "position_rms_cells": _curve(r[:, 0], every),
-            "position_max_cells": _curve(r[:, 1], every), "velocity_rms_rel": _curve(r[:, 2], every),
-            "kinetic_energy_rel": _curve(r[:, 3], every), "fluid_cells_diff": [int(x) for x in r[every - 1::every, 4]]}
+            "tracked_particles": int(tracked.size), "sampled_every": sample,
+            "position_rms_cells": [float(f"{x:.3g}") for x in np.sqrt((dpos ** 2).mean(axis=1))],
+            "position_max_cells": [float(f"{x:.3g}") for x in dpos.max(axis=1)],
+            "velocity_rms_rel": [float(f"{x:.3g}") for x in dvel],
+            "kinetic_energy_rel": _curve(ke, every),
+            "fluid_cells_diff": [int(x) for x in (stats[:, 0] - rs[:, 0])[every - 1::every]]}
 
 
 def drift_dam128(N, every=10):
@@ -535,21 +536,6 @@ def drift_dam128(N, every=10):
         out[name]["oracle_pcg_iterations_mean"] = round(float(gold[f"{name}_stats"][:, 6].mean()), 2)
     ref = gold["flip_threads8_stats"]
     out["fp64_threads"] = compare(ref, gold["flip_threads8_pos"], gold["flip_threads8_vel"], "flip")
-    # CPU side of the same workload: the oracle (APIC, all host threads), 2 timed steps after 1
-    from oracle import oracle as O
-
-    O.build_port()
-    o = O.Oracle(O.make_params(res, transfer=O.APIC, tol=1e-6, max_iters=200), pos.astype(np.float64), lib="port")
-    threads = os.cpu_count() or 1
-    o.set_threads(threads)
-    o.step(dt)
-    t0 = time.perf_counter()
-    for _ in range(2):
-        o.step(dt)
-    c_s = (time.perf_counter() - t0) / 2
-    o.close()
-    out["cpu_port_apic"] = {"steps_per_s": round(1.0 / c_s, 3), "threads": threads,
-                            "sample": "2 steps after 1 of the APIC dam break from the seeded start"}
     return out
 
 
@@ -794,6 +780,34 @@ def cpu_baseline(res: int, dt: float, steps: int = 1, warm: int = 0):
             "sample": f"{steps} full step(s) of {WORKLOAD} ({n} particles) after {warm} warm-up, "
                       f"FP64 oracle, OpenMP x{cores}, MIC(0) PCG iterations {its[warm:]}",
             "seconds_per_step": round(sec, 3)}
+
+
+def cpu_baseline_configs():
+    """The oracle (FP64, all host threads) on the smaller dam-break
+    configurations: 32^3 FLIP (dt 1/120; 20 steps after 3) and 128^3 APIC
+    (dt 1/240; 2 steps after 1), from the seeded start."""
+    from fluid_simulator_gb300.scenes import GridSpec, dam_break
+    from oracle import oracle as O
+
+    O.build_port()
+    threads = os.cpu_count() or 1
+    out = {}
+    for name, res, transfer, dt, warm, steps in (("dam32_flip", 32, O.FLIP, 1.0 / 120.0, 3, 20),
+                                                 ("dam128_apic", 128, O.APIC, 1.0 / 240.0, 1, 2)):
+        pos = dam_break(GridSpec(res), seed=0)
+        o = O.Oracle(O.make_params(res, transfer=transfer, tol=1e-6, max_iters=200), pos.astype(np.float64),
+                     lib="port")
+        o.set_threads(threads)
+        for _ in range(warm):
+            o.step(dt)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            o.step(dt)
+        sec = (time.perf_counter() - t0) / steps
+        o.close()
+        out[name] = {"steps_per_s": round(1.0 / sec, 3), "threads": threads,
+                     "sample": f"{steps} steps after {warm} from the seeded start"}
+    return out
 
 
 def run_solve_case(args):
