@@ -401,11 +401,12 @@ def run_fsim(args):
                 "publish_alone_d2h_gbs": round(pub_bytes / pub_s / 1e9, 1)},
         "gpu_launches": int(sum(s.kernel_launches for s in stats)),
     }
-    if args.precision_study:
+    # the studies are single-GPU diagnostics outside the timed region: N = 1 only
+    if args.precision_study and world == 1:
         line["pcg_precision"] = precision_study(sim, N)
-    if args.ws_steps > 0:
+    if args.ws_steps > 0 and world == 1:
         line["pcg_warm_start"] = warm_start_study(sim, dt, t, h, N, args)
-    if args.render:
+    if args.render and world == 1:
         line["render"] = render_study(sim, N, h, peak)
     sim.close()
     if args.parity and rank == 0 and world == 1:
